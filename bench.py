@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""DUGKS D3Q19 step throughput (MLUPS) on GB300.
+
+Workload: turbulent channel at Re_tau = 180, 256 (streamwise) x 128 (wall-
+normal, tanh-stretched, first cell centre at y+ = 0.5) x 128 (spanwise)
+cells, in the reference orientation (walls on the x faces, streamwise z:
+nx=128, ny=128, nz=256).  Seeded synthetic initial state (laminar profile +
+perturbations + near-wall streaks); the reference's Zenodo restart dumps are
+not available.  A step is one full DUGKS step (stage (a) f-bar-plus, ghost
+formation, reconstruction, face fluxes, update) over the whole grid.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|fp32|fp16|bf16]
+  python bench.py --impl reference ...   # the step on the host cores (CPU port of the reference)
+
+Prints one JSON line (rank 0).  Under torchrun (N>1) every rank advances its
+own replica (the step does not shard across GPUs here): weak scaling, no
+data-path collective.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "dugks-gpu_gb300"))
+
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--precision", default="fp64", choices=("fp64", "fp32", "fp16", "bf16"))
+    ap.add_argument("--grid", default="128,128,256", help="nx,ny,nz in the reference orientation")
+    ap.add_argument("--no-extras", action="store_true", help="skip the CPU baseline, other forms and reference-GPU legs")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(args, precision):
+    import pydugks
+    nx, ny, nz = (int(v) for v in args.grid.split(","))
+    cfg, meta = pydugks.channel_config(nx=nx, ny=ny, nz=nz, precision=precision)
+    return cfg, meta, (nx, ny, nz)
+
+
+def describe(grid, precision):
+    nx, ny, nz = grid
+    return (f"DUGKS D3Q19 turbulent channel Re_tau=180, {nz}(streamwise) x {nx}(wall-normal, tanh-stretched) x "
+            f"{ny}(spanwise), {precision}")
+
+
+class ClockSampler:
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={CLOCK_FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), float(parts[3]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = sorted(r[0] for r in rows)
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[3]) if v.lower().startswith("active")})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+def measured_peak_hbm():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(precision):
+    """DRAM bytes per flux launch from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        d = json.load(open(p))
+        return d.get(precision)
+    except Exception:
+        return None
+
+
+def time_steps(eng, istep0, k):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    ms_a, ms_b = eng.run_profiled(istep0, k)
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1), ms_a, ms_b
+
+
+def run_form(args, precision, k, w):
+    """Device-resident timing of one form; returns (MLUPS, ms/step, ms_a, ms_b)."""
+    import pydugks
+    import torch
+    cfg, _, grid = workload(args, precision)
+    with pydugks.Engine(cfg) as eng:
+        eng.set_stream(torch.cuda.current_stream().cuda_stream)
+        eng.run(1, w)
+        eng.sync()
+        ms, ms_a, ms_b = time_steps(eng, w + 1, k)
+        n = grid[0] * grid[1] * grid[2]
+        return n * k / (ms / 1e3) / 1e6, ms / k, ms_a / k, ms_b / k
+
+
+def cpu_baseline(args, budget_s=12.0):
+    """The oracle (CPU port of the reference step, OpenMP over all host cores) on
+    the same workload; a bounded number of full-grid steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pydugks
+    import pyoracle
+    cfg, _, grid = workload(args, "fp64")
+    eng = pydugks.Engine(cfg)
+    f0 = eng.get_state()
+    xc, dxx = eng.mesh()
+    orc = pyoracle.Oracle.from_engine_info(eng.info, xc=xc, dxx=dxx)
+    eng.close()
+    g = pyoracle.to_ghosted(f0)
+    del f0
+    threads = pyoracle.max_threads()
+    t = time.perf_counter()
+    orc.run(g, 1, 1, threads)
+    t1 = time.perf_counter() - t
+    steps = max(1, min(50, int(budget_s / max(t1, 1e-3))))
+    t = time.perf_counter()
+    orc.run(g, 2, steps, threads)
+    dt = time.perf_counter() - t
+    n = grid[0] * grid[1] * grid[2]
+    return {"value": n * steps / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{steps} full-grid FP64 steps of the same workload (after 1 untimed step), "
+                      f"oracle/dugks_oracle.c with OpenMP"}
+
+
+def reference_gpu(args, k=10):
+    """The reference's own CUDA-C kernels (oracle/_ref cubin) on the uniform-mesh
+    variant of the same grid (the reference has no stretched mesh)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import pyoracle
+    if not pyoracle.ref_cubins_present():
+        return None
+    nx, ny, nz = (int(v) for v in args.grid.split(","))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from seeded import seeded_state  # noqa: E402
+    f = pyoracle.to_ghosted(seeded_state(nx, ny, nz, seed=0, umax=0.05, eps=0.001))
+    ms = pyoracle.ref_run(f, nx, ny, nz, 0.5, float(nx), float(np.float32(268.0826)), float(np.float32(804.2477)),
+                          float(np.float32(0.00227007141)), (0.0, 0.0, float(np.float32(6.36918888e-07))),
+                          periods=(0, 1, 1), istep0=1, nsteps=2, prec=0)
+    ms = pyoracle.ref_run(f, nx, ny, nz, 0.5, float(nx), float(np.float32(268.0826)), float(np.float32(804.2477)),
+                          float(np.float32(0.00227007141)), (0.0, 0.0, float(np.float32(6.36918888e-07))),
+                          periods=(0, 1, 1), istep0=3, nsteps=k, prec=0)
+    return {"value": nx * ny * nz / (ms / 1e3) / 1e6, "unit": "MLUPS", "ms_per_step": ms, "steps": k,
+            "what": "reference src/dugks.cu kernels (unmodified, nvcc sm_103a), FP64, uniform-mesh variant of the grid"}
+
+
+def main_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import pydugks  # noqa: F401
+    import pyoracle
+    cfg, _, grid = workload(args, "fp64")
+    # the initial state and mesh come from the same generator the GPU arm uses
+    eng = pydugks.Engine(cfg)
+    f0 = eng.get_state()
+    xc, dxx = eng.mesh()
+    orc = pyoracle.Oracle.from_engine_info(eng.info, xc=xc, dxx=dxx)
+    eng.close()
+    g = pyoracle.to_ghosted(f0)
+    del f0
+    threads = pyoracle.max_threads()
+    orc.run(g, 1, args.warmup, threads)
+    t = time.perf_counter()
+    orc.run(g, args.warmup + 1, args.steps, threads)
+    dt = time.perf_counter() - t
+    n = grid[0] * grid[1] * grid[2]
+    value = n * args.steps / dt / 1e6
+    line = {"impl": "reference", "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": describe(grid, "fp64"), "grid": list(grid), "mesh": "tanh",
+                       "parallelism": "host OpenMP"},
+            "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} full-grid FP64 steps after {args.warmup} warm-up steps; "
+                                       "the reference has no CPU path, so this is the oracle's restatement of "
+                                       "its step (oracle/dugks_oracle.c, OpenMP)"},
+            "e2e": {"value": value, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_extras:
+        try:
+            line["reference_gpu"] = reference_gpu(args)
+        except Exception as e:
+            line["reference_gpu"] = f"error: {e}"
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        return main_reference(args)
+    import numpy as np
+    import torch
+    import pydugks
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    cfg, meta, grid = workload(args, args.precision)
+    n = grid[0] * grid[1] * grid[2]
+    K, W = args.steps, max(3, args.warmup)
+
+    eng = pydugks.Engine(cfg)
+    eng.set_stream(torch.cuda.current_stream().cuda_stream)
+    eng.run(1, W)
+    eng.sync()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    ms, ms_a, ms_b = time_steps(eng, W + 1, K)
+    clocks = sampler.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n * K / (ms / 1e3) / 1e6
+
+    # end to end through the C ABI with host buffers: upload the state from
+    # pinned host memory, K steps each followed by a host read of the step's
+    # conserved moments, download the final state
+    state_bytes = n * 19 * 8
+    h_in = torch.empty(n * 19, dtype=torch.float64, pin_memory=True).numpy()
+    h_out = torch.empty(n * 19, dtype=torch.float64, pin_memory=True).numpy()
+    h_in[:] = eng.get_state().ravel()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    eng.set_state(h_in)
+    for s in range(K):
+        eng.step(W + K + 1 + s)
+        eng.moments()
+    pydugks.lib().dg_get_state(eng._h, h_out.ctypes.data_as(pydugks._D))
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": n * K / e2e_s / 1e6, "unit": "MLUPS",
+           "h2d_bytes_per_step": state_bytes / K,
+           "d2h_bytes_per_step": state_bytes / K + 304 * 4 * 8,
+           "what": "dg_set_state(pinned host) + K x (dg_step + dg_moments host read) + dg_get_state(pinned host)"}
+    eng.close()
+
+    info_bytes = {"fp64": 8, "fp32": 4, "fp16": 2, "bf16": 2}[args.precision]
+    flux_bytes = 57 * info_bytes * n
+    achieved = flux_bytes / (ms_b / K / 1e3) / 1e9
+    peak, peak_kind = measured_peak_hbm()
+    roof = {"bound": "hbm", "kernel": "flux_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": ncu_traffic(args.precision),
+            "peak_source": peak_kind, "alg_bytes_per_cell": 57 * info_bytes,
+            "kernel_ms": {"fbar_kernel": ms_a / K, "flux_kernel": ms_b / K},
+            "step_alg_bytes_per_cell": 95 * info_bytes,
+            "step_frac": 95 * info_bytes * n * K / (ms / 1e3) / 1e9 / peak}
+
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras:
+        forms = {}
+        for p in ("fp64", "fp32", "fp16", "bf16"):
+            if p == args.precision:
+                forms[p] = value
+                continue
+            try:
+                forms[p] = run_form(args, p, K, W)[0]
+            except Exception as e:  # report, do not hide
+                forms[p] = f"error: {e}"
+        extras["forms_mlups"] = forms
+        try:
+            extras["cpu_baseline"] = cpu_baseline(args)
+        except Exception as e:
+            extras["cpu_baseline"] = {"error": str(e)}
+
+    if rank == 0:
+        line = {"metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
+                "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": {"fp64": "f64", "fp32": "f32", "fp16": "f16-storage/f32", "bf16": "bf16-storage/f32"}[args.precision],
+                "data": "synthetic",
+                "config": {"workload": describe(grid, args.precision), "grid_nx_ny_nz": list(grid), "mesh": "tanh",
+                           "re_tau": 180, "nu": meta["nu"], "alpha": meta["alpha"], "parallelism": f"replicas x{world}",
+                           "l2": "inputs larger than L2 (f and f-bar-plus resident, %d MB each)" % (n * 19 * info_bytes // 2**20),
+                           "structure": "two-pass (stage a kernel, flux+update kernel)"},
+                "e2e": e2e, "gpu_launches": 2 * K, "roofline": roof, "clocks": clocks}
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

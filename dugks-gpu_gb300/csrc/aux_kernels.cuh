@@ -1,0 +1,114 @@
+// Auxiliary kernels: state transposes between the host dump order and the
+// device SoA storage, deterministic statistics partial sums, conserved
+// moments.  Templated on arithmetic type T and storage type S like the step.
+#pragma once
+#include "dugks_kernels.cuh"
+
+namespace dg {
+
+// dump order f[((k*ny+j)*nx+i)*19+p] (double)  ->  SoA storage
+template <class T, class S>
+__global__ void __launch_bounds__(256) aos_to_soa_kernel(const double *__restrict__ src, S *__restrict__ dst,
+                                                         const StepParams<T, S> P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    if (i >= P.nx) return;
+    const size_t cell = ((size_t)k * P.ny + j) * P.nx + i;
+    const long long c = ((long long)k * P.ny + j) * P.pitch + i;
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) P.codec.store(dst, p * P.ps + c, p, T(src[cell * NPOP + p]));
+}
+
+// SoA storage -> dump order (double)
+template <class T, class S>
+__global__ void __launch_bounds__(256) soa_to_aos_kernel(const S *__restrict__ src, double *__restrict__ dst,
+                                                         const StepParams<T, S> P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    if (i >= P.nx) return;
+    const size_t cell = ((size_t)k * P.ny + j) * P.nx + i;
+    const long long c = ((long long)k * P.ny + j) * P.pitch + i;
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) dst[cell * NPOP + p] = double(P.codec.load_nc(src, p * P.ps + c, p));
+}
+
+// Number of FP64 partial sums per x index written by stats_partials_kernel:
+//  0 rho, 1 u, 2 v, 3 w, 4 uw, 5 uv, 6 vw, 7 uu, 8 vv, 9 ww,
+//  10..13 min rho,u,v,w, 14..17 max rho,u,v,w, 18 non-finite count
+constexpr int NSTAT = 19;
+
+// Block (b, by) sums rows (j,k) = b, b+gridDim.x, ... ; thread owns x index
+// i = by*blockDim.x + threadIdx.x.  Output partial[b][i][NSTAT].  The fixed assignment and
+// the ordered second pass make the result independent of scheduling.
+template <class T, class S>
+__global__ void __launch_bounds__(1024) stats_partials_kernel(const S *__restrict__ f, const StepParams<T, S> P,
+                                                              double hdt, double fxa, double fya, double fza,
+                                                              double *__restrict__ partial)
+{
+    const int i = blockIdx.y * blockDim.x + threadIdx.x;
+    if (i >= P.nx) return;
+    double acc[NSTAT];
+#pragma unroll
+    for (int s = 0; s < 10; ++s) acc[s] = 0.0;
+#pragma unroll
+    for (int s = 10; s < 14; ++s) acc[s] = 1e300;
+#pragma unroll
+    for (int s = 14; s < 18; ++s) acc[s] = -1e300;
+    acc[18] = 0.0;
+    const int rows = P.ny * P.nz;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        const long long c = (long long)row * P.pitch + i;
+        double v[NPOP];
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) v[p] = double(P.codec.load_nc(f, p * P.ps + c, p));
+        double r, jx, jy, jz;
+        moments(v, r, jx, jy, jz);
+        const double u = jx / r + fxa * hdt, vv = jy / r + fya * hdt, w = jz / r + fza * hdt;
+        if (!isfinite(r) || !isfinite(u) || !isfinite(vv) || !isfinite(w)) acc[18] += 1.0;
+        acc[0] += r; acc[1] += u; acc[2] += vv; acc[3] += w;
+        acc[4] += u * w; acc[5] += u * vv; acc[6] += vv * w;
+        acc[7] += u * u; acc[8] += vv * vv; acc[9] += w * w;
+        acc[10] = fmin(acc[10], r); acc[11] = fmin(acc[11], u); acc[12] = fmin(acc[12], vv); acc[13] = fmin(acc[13], w);
+        acc[14] = fmax(acc[14], r); acc[15] = fmax(acc[15], u); acc[16] = fmax(acc[16], vv); acc[17] = fmax(acc[17], w);
+    }
+    double *out = partial + ((size_t)blockIdx.x * P.nx + i) * NSTAT;
+#pragma unroll
+    for (int s = 0; s < NSTAT; ++s) out[s] = acc[s];
+}
+
+// Ordered reduction over blocks: total[i][s] = sum/min/max over b of partial[b][i][s].
+__global__ void stats_reduce_kernel(const double *__restrict__ partial, int nblocks, int nx, double *__restrict__ total);
+
+// Conserved moments: block partial sums of (rho, jx, jy, jz) over cells.
+template <class T, class S>
+__global__ void __launch_bounds__(256) moments_partials_kernel(const S *__restrict__ f, const StepParams<T, S> P,
+                                                               double *__restrict__ partial)
+{
+    __shared__ double red[4][256];
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    const long long ncell = (long long)P.nx * P.ny * P.nz;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < ncell; q += (long long)gridDim.x * blockDim.x) {
+        const long long row = q / P.nx;
+        const int i = int(q - row * P.nx);
+        const long long c = row * P.pitch + i;
+        double v[NPOP];
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) v[p] = double(P.codec.load_nc(f, p * P.ps + c, p));
+        double r, jx, jy, jz;
+        moments(v, r, jx, jy, jz);
+        a0 += r; a1 += jx; a2 += jy; a3 += jz;
+    }
+    red[0][threadIdx.x] = a0; red[1][threadIdx.x] = a1; red[2][threadIdx.x] = a2; red[3][threadIdx.x] = a3;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int m = 0; m < 4; ++m) red[m][threadIdx.x] += red[m][threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int m = 0; m < 4; ++m) partial[blockIdx.x * 4 + m] = red[m][0];
+}
+
+}  // namespace dg

@@ -1,0 +1,63 @@
+// Storage codecs for the distribution arrays.
+//
+//   Codec<double, double>, Codec<float, float>: plain values (FP64 / FP32 forms)
+//   Codec<float, __half>, Codec<float, __nv_bfloat16>: 16-bit deviations from
+//       the rest-state equilibrium, d_p = (f_p - w_p) / s_p, with one scale s_p
+//       per population; decoded and re-encoded in FP32 (the mixed form).
+#pragma once
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+#include "d3q19.cuh"
+
+namespace dg {
+
+template <class T, class S>
+struct Codec {
+    __device__ __forceinline__ T load(const S *a, long long idx, int) const { return T(a[idx]); }
+    __device__ __forceinline__ T load_nc(const S *a, long long idx, int) const { return T(__ldg(a + idx)); }
+    __device__ __forceinline__ void store(S *a, long long idx, int, T v) const { a[idx] = S(v); }
+    static constexpr bool deviation = false;
+};
+
+template <class S>
+struct DevCodec {
+    float w[NPOP];    // rest-state equilibrium w_p (feq(rho=1, u=0))
+    float s[NPOP];    // scale s_p
+    float is[NPOP];   // 1 / s_p
+    static constexpr bool deviation = true;
+};
+
+template <>
+struct Codec<float, __half> : DevCodec<__half> {
+    __device__ __forceinline__ float load(const __half *a, long long idx, int p) const
+    {
+        return fmaf(s[p], __half2float(a[idx]), w[p]);
+    }
+    __device__ __forceinline__ float load_nc(const __half *a, long long idx, int p) const
+    {
+        return fmaf(s[p], __half2float(__ldg(a + idx)), w[p]);
+    }
+    __device__ __forceinline__ void store(__half *a, long long idx, int p, float v) const
+    {
+        a[idx] = __float2half_rn((v - w[p]) * is[p]);
+    }
+};
+
+template <>
+struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
+    __device__ __forceinline__ float load(const __nv_bfloat16 *a, long long idx, int p) const
+    {
+        return fmaf(s[p], __bfloat162float(a[idx]), w[p]);
+    }
+    __device__ __forceinline__ float load_nc(const __nv_bfloat16 *a, long long idx, int p) const
+    {
+        return fmaf(s[p], __bfloat162float(__ldg(a + idx)), w[p]);
+    }
+    __device__ __forceinline__ void store(__nv_bfloat16 *a, long long idx, int p, float v) const
+    {
+        a[idx] = __float2bfloat16_rn((v - w[p]) * is[p]);
+    }
+};
+
+}  // namespace dg

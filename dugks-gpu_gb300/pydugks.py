@@ -1,0 +1,286 @@
+"""ctypes binding of the dugks_gb300 C ABI (include/dugks_gb300.h).
+
+The Python-facing mirror of the reference's solver interface
+(Kairzhan/DUGKS-GPU src/dugks.h:1-9, src/output.h:1-5): an `Engine` owns one
+`dg_t` handle.  Every call goes through libdugks_gb300.so; there is no Python
+or CPU implementation of the step behind it, and importing this module fails
+loudly when the library has not been built.
+
+Host arrays are numpy float64:
+  state (dump order):  shape (nz, ny, nx, 19)   -- ddf%08d.dat element order
+  ghosted macro:       shape (nz+2, ny+2, nx+2)
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdugks_gb300.so")
+
+DG_OK = 0
+DG_ERR_CONFIG = -1
+DG_ERR_IO = -2
+DG_ERR_SHAPE = -3
+DG_ERR_CUDA = -4
+DG_ERR_NUMERIC = -5
+DG_ERR_ARG = -6
+DG_ERR_UNSUPPORTED = -7
+
+PREC = {"fp64": 0, "fp32": 1, "fp16": 2, "bf16": 3}
+
+# Keys read by the reference (src/numerics.cu:70-99, src/parallel.cu:95-97,
+# src/cuda.cu:17), in the order of examples/laminar/config.txt.
+REFERENCE_KEYS = ("case", "xwidth", "ywidth", "zwidth", "nx", "ny", "nz", "restart", "nrestart", "perturb",
+                  "istep0", "nsteps", "noutput3", "noutput2", "ndump", "CFL", "visc", "ambient_fx",
+                  "ambient_fy", "ambient_fz", "periods_x", "periods_y", "periods_z", "gpusPerThread")
+
+
+class DugksError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"dugks_gb300 status {code}: {message}")
+        self.code = code
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("pitch", ctypes.c_int),
+                ("pop_stride", ctypes.c_longlong), ("precision", ctypes.c_int),
+                ("periodic", ctypes.c_int * 3), ("mesh", ctypes.c_int), ("recon", ctypes.c_int),
+                ("perturb", ctypes.c_int), ("istep0", ctypes.c_int), ("nsteps", ctypes.c_int),
+                ("noutput2", ctypes.c_int), ("ndump", ctypes.c_int), ("restart", ctypes.c_int),
+                ("nrestart", ctypes.c_int), ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+                ("dz", ctypes.c_double), ("dt", ctypes.c_double), ("visc", ctypes.c_double),
+                ("tau", ctypes.c_double), ("xwidth", ctypes.c_double), ("ywidth", ctypes.c_double),
+                ("zwidth", ctypes.c_double), ("ambient", ctypes.c_double * 3), ("bw0", ctypes.c_double),
+                ("bw1", ctypes.c_double), ("bw2", ctypes.c_double), ("fw0", ctypes.c_double),
+                ("fw1", ctypes.c_double), ("fw2", ctypes.c_double), ("hbm_bytes_per_cell", ctypes.c_double)]
+
+
+_lib = None
+_D = ctypes.POINTER(ctypes.c_double)
+
+
+def lib():
+    """Load libdugks_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(LIB_PATH)
+    H = ctypes.c_void_p
+    sig = {
+        "dg_create": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(H)]),
+        "dg_create_from_text": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.POINTER(H)]),
+        "dg_destroy": (ctypes.c_int, [H]),
+        "dg_last_error": (ctypes.c_char_p, [H]),
+        "dg_get_info": (ctypes.c_int, [H, ctypes.POINTER(Info)]),
+        "dg_set_stream": (ctypes.c_int, [H, ctypes.c_void_p]),
+        "dg_step": (ctypes.c_int, [H, ctypes.c_int]),
+        "dg_run": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_int]),
+        "dg_run_profiled": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_int, _D]),
+        "dg_sync": (ctypes.c_int, [H]),
+        "dg_upload_macro": (ctypes.c_int, [H]),
+        "dg_copy_vel": (ctypes.c_int, [H, _D, _D, _D, _D]),
+        "dg_stats_values": (ctypes.c_int, [H, _D, _D]),
+        "dg_stats": (ctypes.c_int, [H, ctypes.c_int]),
+        "dg_output_2d": (ctypes.c_int, [H, ctypes.c_int]),
+        "dg_copy_ddf": (ctypes.c_int, [H, _D]),
+        "dg_get_state": (ctypes.c_int, [H, _D]),
+        "dg_set_state": (ctypes.c_int, [H, _D]),
+        "dg_dump": (ctypes.c_int, [H, ctypes.c_int]),
+        "dg_read_dump": (ctypes.c_int, [H, ctypes.c_int]),
+        "dg_device_ptr": (ctypes.c_void_p, [H, ctypes.c_int]),
+        "dg_moments": (ctypes.c_int, [H, _D]),
+        "dg_get_mesh": (ctypes.c_int, [H, _D, _D]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(_D)
+
+
+def make_config(**kw):
+    """Reference-format config.txt text; every reference key gets a default.
+
+    Extension keys of this engine (precision, mesh, mesh_alpha, mesh_file,
+    recon, ub, re_tau, seed, ...) are appended when given."""
+    d = dict(case="channel", xwidth=64, ywidth=32, zwidth=32, nx=64, ny=32, nz=32, restart=0, nrestart=0,
+             perturb=0, istep0=1, nsteps=100, noutput3=10000000, noutput2=5000, ndump=100000, CFL=0.7,
+             visc=0.166, ambient_fx=0.0, ambient_fy=0.0, ambient_fz=3.2421875e-5, periods_x=0, periods_y=1,
+             periods_z=1, gpusPerThread=8)
+    d.update(kw)
+    lines = ["#####################"]
+    for k in REFERENCE_KEYS:
+        lines.append(f"{k}={d.pop(k)}")
+    for k, v in d.items():
+        lines.append(f"{k}={v}")
+    return "\n".join(lines) + "\n"
+
+
+def tanh_alpha_for_first_face(nx, L, x1):
+    """alpha of the tanh mesh (src/fortran/channel/run/mesh.py:21-25) whose first
+    face lies at x1 from the wall (bisection; the first face moves towards the
+    wall as alpha grows)."""
+    import math
+    lo, hi = 1e-9, 1 - 1e-12
+    eta = -1.0 + 2.0 / nx
+    for _ in range(200):
+        a = 0.5 * (lo + hi)
+        xf1 = L / (2 * a) * math.tanh(eta * 0.5 * (math.log(1 + a) - math.log(1 - a))) + 0.5 * L
+        if xf1 > x1:
+            lo = a
+        else:
+            hi = a
+    return 0.5 * (lo + hi)
+
+
+def channel_config(nx=128, ny=128, nz=256, precision="fp64", re_tau=180.0, ub=0.1, yplus1=0.5, cfl=0.5,
+                   seed=0, **extra):
+    """Turbulent channel at Re_tau in the reference orientation: walls on the
+    x faces (tanh-stretched, nx cells across 2H = xwidth = nx), spanwise y,
+    streamwise z with the body force.  Domain 2H x (4/3)pi H x 4 pi H.
+    nu from the bulk velocity ub through Dean's correlation
+    Re_tau = 0.09 Re_b^0.88 (Re_b = 2 H ub / nu); u_tau = Re_tau nu / H;
+    F = u_tau^2 / H; the mesh alpha puts the first cell centre at y+ = yplus1.
+    Initial state: case=channel_turb (laminar profile + seeded perturbations
+    of +-10% ub + near-wall streaks of 5% ub)."""
+    import math
+    H = nx / 2.0
+    re_b = (re_tau / 0.09) ** (1.0 / 0.88)
+    nu = 2 * H * ub / re_b
+    utau = re_tau * nu / H
+    F = utau * utau / H
+    alpha = tanh_alpha_for_first_face(nx, 2 * H, 2 * yplus1 * H / re_tau)
+    kw = dict(case="channel_turb", nx=nx, ny=ny, nz=nz, xwidth=2 * H, ywidth=round(4.0 / 3.0 * math.pi * H, 4),
+              zwidth=round(4.0 * math.pi * H, 4), periods_x=0, CFL=cfl, visc=f"{nu:.9g}", ambient_fz=f"{F:.9g}",
+              mesh="tanh", mesh_alpha=f"{alpha:.15g}", precision=precision, ub=ub, re_tau=re_tau, seed=seed,
+              noutput2=1000, ndump=100000, nsteps=50000)
+    kw.update(extra)
+    return make_config(**kw), dict(nu=nu, utau=utau, F=F, alpha=alpha, re_b=re_b)
+
+
+def last_error(h=None):
+    return lib().dg_last_error(h).decode(errors="replace")
+
+
+class Engine:
+    """One dg_t handle.  `config` is config.txt text; files go to `workdir`."""
+
+    def __init__(self, config=None, workdir=".", config_path=None):
+        L = lib()
+        h = ctypes.c_void_p()
+        if config_path is not None:
+            rc = L.dg_create(config_path.encode(), ctypes.byref(h))
+        else:
+            rc = L.dg_create_from_text(config.encode(), workdir.encode(), ctypes.byref(h))
+        if rc != DG_OK:
+            raise DugksError(rc, last_error(None))
+        self._h = h
+        self.info = Info()
+        self._check(L.dg_get_info(self._h, ctypes.byref(self.info)))
+        self.nx, self.ny, self.nz = self.info.nx, self.info.ny, self.info.nz
+
+    def _check(self, rc):
+        if rc != DG_OK:
+            raise DugksError(rc, last_error(self._h))
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().dg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # stepping
+    def step(self, istep):
+        self._check(lib().dg_step(self._h, istep))
+
+    def run(self, istep0, nsteps):
+        self._check(lib().dg_run(self._h, istep0, nsteps))
+
+    def run_profiled(self, istep0, nsteps):
+        """Run with per-kernel CUDA events; returns (ms of stage (a), ms of flux) summed over the steps."""
+        ms = np.zeros(2)
+        self._check(lib().dg_run_profiled(self._h, istep0, nsteps, _ptr(ms)))
+        return float(ms[0]), float(ms[1])
+
+    def sync(self):
+        self._check(lib().dg_sync(self._h))
+
+    def set_stream(self, stream_handle):
+        self._check(lib().dg_set_stream(self._h, ctypes.c_void_p(stream_handle)))
+
+    # state
+    def get_state(self):
+        a = np.empty((self.nz, self.ny, self.nx, 19), dtype=np.float64)
+        self._check(lib().dg_get_state(self._h, _ptr(a)))
+        return a
+
+    def set_state(self, a):
+        a = np.ascontiguousarray(a, dtype=np.float64).reshape(self.nz, self.ny, self.nx, 19)
+        self._check(lib().dg_set_state(self._h, _ptr(a)))
+
+    def copy_ddf(self):
+        a = np.empty((self.nz + 2, self.ny + 2, self.nx + 2, 19), dtype=np.float64)
+        self._check(lib().dg_copy_ddf(self._h, _ptr(a)))
+        return a
+
+    def dump(self, step):
+        self._check(lib().dg_dump(self._h, step))
+
+    def read_dump(self, step):
+        self._check(lib().dg_read_dump(self._h, step))
+
+    # macro / statistics
+    def copy_vel(self):
+        shape = (self.nz + 2, self.ny + 2, self.nx + 2)
+        out = [np.empty(shape, dtype=np.float64) for _ in range(4)]
+        self._check(lib().dg_copy_vel(self._h, *[_ptr(a) for a in out]))
+        return out
+
+    def stats_values(self):
+        diag = np.empty(12, dtype=np.float64)
+        prof = np.empty((self.nx, 9), dtype=np.float64)
+        self._check(lib().dg_stats_values(self._h, _ptr(diag), _ptr(prof)))
+        return diag, prof
+
+    def stats(self, step):
+        self._check(lib().dg_stats(self._h, step))
+
+    def output_2d(self, step):
+        self._check(lib().dg_output_2d(self._h, step))
+
+    def moments(self):
+        m = np.empty(4, dtype=np.float64)
+        self._check(lib().dg_moments(self._h, _ptr(m)))
+        return m
+
+    def mesh(self):
+        xc = np.empty(self.nx + 2)
+        dxx = np.empty(self.nx + 2)
+        self._check(lib().dg_get_mesh(self._h, _ptr(xc), _ptr(dxx)))
+        return xc, dxx
+
+    def device_ptr(self, which):
+        return lib().dg_device_ptr(self._h, which)

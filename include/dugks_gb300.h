@@ -1,0 +1,166 @@
+/*
+ * dugks_gb300 -- C ABI of the GB300-native D3Q19 DUGKS time-step engine.
+ *
+ * A handle-based replacement for the reference's module-global solver
+ * interface (Kairzhan/DUGKS-GPU src/dugks.h:1-9, src/output.h:1-5).  Plain
+ * pointers and sizes only; every call returns an int status (DG_OK == 0,
+ * negative on error) and never exits the process.  One handle per host
+ * thread; a handle owns all of its device memory and frees it in
+ * dg_destroy().
+ *
+ * Host-side arrays exchanged through this interface are always double,
+ * whatever the engine's storage precision.  Layouts:
+ *   - "ghosted AoS" (the reference's h_f, src/dugks.cu:15-17):
+ *       f[((k*(ny+2)+j)*(nx+2)+i)*19+ip], 0<=i<nx+2 ...
+ *   - "dump order" (ddf%08d.dat, src/output.cu:22-41):
+ *       f[((k*ny+j)*nx+i)*19+ip], interior cells only
+ *   - "ghosted scalar" (h_rho, h_ux ..., src/dugks.cu:204-207):
+ *       a[(k*(ny+2)+j)*(nx+2)+i]
+ */
+#ifndef DUGKS_GB300_H
+#define DUGKS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct dg_ctx dg_t;
+
+/* status codes */
+#define DG_OK 0
+#define DG_ERR_CONFIG (-1)      /* missing / malformed config key */
+#define DG_ERR_IO (-2)          /* file missing, short or oversized */
+#define DG_ERR_SHAPE (-3)       /* grid sizes / buffer sizes inconsistent */
+#define DG_ERR_CUDA (-4)        /* a CUDA runtime call or launch failed */
+#define DG_ERR_NUMERIC (-5)     /* NaN / Inf detected in the state */
+#define DG_ERR_ARG (-6)         /* NULL handle or pointer, bad enum */
+#define DG_ERR_UNSUPPORTED (-7) /* boundary / option the engine does not implement */
+
+/* storage / arithmetic forms (config key `precision`) */
+#define DG_PREC_FP64 0          /* FP64 storage and arithmetic (parity mode) */
+#define DG_PREC_FP32 1          /* FP32 storage and arithmetic */
+#define DG_PREC_FP16 2          /* FP16 deviation storage, FP32 arithmetic */
+#define DG_PREC_BF16 3          /* BF16 deviation storage, FP32 arithmetic */
+
+/* device buffers exposed read-only (dg_device_ptr) */
+#define DG_BUF_F 0              /* f-tilde, structure of arrays */
+#define DG_BUF_FB 1             /* f-bar-plus, structure of arrays */
+#define DG_BUF_RHO 2            /* ghosted scalar macro arrays (after dg_upload_macro) */
+#define DG_BUF_UX 3
+#define DG_BUF_UY 4
+#define DG_BUF_UZ 5
+
+typedef struct {
+    int nx, ny, nz;             /* interior cells */
+    int pitch;                  /* x pitch of the device SoA arrays, elements */
+    long long pop_stride;       /* elements between populations in the device SoA arrays */
+    int precision;              /* DG_PREC_* */
+    int periodic[3];            /* periods_x/y/z */
+    int mesh;                   /* 0 uniform, 1 tanh-stretched x, 2 x faces from a mesh file */
+    int recon;                  /* 0 trilinear, 1 central-difference gradient */
+    int perturb;                /* calc_perturb_force active */
+    int istep0, nsteps, noutput2, ndump, restart, nrestart;
+    double dx, dy, dz, dt, visc, tau;
+    double xwidth, ywidth, zwidth;
+    double ambient[3];
+    double bw0, bw1, bw2, fw0, fw1, fw2;
+    double hbm_bytes_per_cell;  /* algorithmic HBM bytes per cell update of one step */
+} dg_info_t;
+
+/* --- lifetime ---------------------------------------------------------- */
+
+/* Reads a reference config.txt (same keys and std::stof / std::stoi parsing,
+ * src/numerics.cu:62-106, src/parallel.cu:95-97, src/cuda.cu:17), allocates
+ * the device state and sets the initial condition of `case` or, with
+ * restart=1, reads ddf<nrestart>.dat from the config file's directory.
+ * Replaces Numerics::init_numerics + init_parallel + init_cuda + init_dugks
+ * (src/main.cu:16-20, src/dugks.cu:95-302). */
+int dg_create(const char *config_path, dg_t **out);
+
+/* Same, from config text; dumps / statistics files go to `workdir`. */
+int dg_create_from_text(const char *config_text, const char *workdir, dg_t **out);
+
+/* Frees everything the handle owns. */
+int dg_destroy(dg_t *h);
+
+/* Message of the last failing call on this handle (or of the last failing
+ * dg_create* when h is NULL). */
+const char *dg_last_error(const dg_t *h);
+
+int dg_get_info(const dg_t *h, dg_info_t *info);
+
+/* Caller-supplied stream (a cudaStream_t); 0 = legacy default stream. */
+int dg_set_stream(dg_t *h, void *cuda_stream);
+
+/* --- time stepping ----------------------------------------------------- */
+
+/* One DUGKS step (stage a, ghost fill, stages b-e), asynchronous on the
+ * handle's stream.  Replaces dugks_step(int) (src/dugks.cu:322-391). */
+int dg_step(dg_t *h, int istep);
+
+/* Steps istep0 .. istep0+nsteps-1 back to back, asynchronous. */
+int dg_run(dg_t *h, int istep0, int nsteps);
+
+/* dg_run with every launch bracketed by CUDA events on the handle's stream;
+ * waits for completion and returns the summed milliseconds of the stage (a)
+ * launches in kernel_ms[0] and of the flux launches in kernel_ms[1]. */
+int dg_run_profiled(dg_t *h, int istep0, int nsteps, double *kernel_ms);
+
+/* Waits for the handle's stream and reports any pending CUDA error. */
+int dg_sync(dg_t *h);
+
+/* --- macroscopic output and statistics --------------------------------- */
+
+/* rho, u = j/rho + hdt*F on device (src/dugks.cu:311-320, 1021-1064). */
+int dg_upload_macro(dg_t *h);
+
+/* Copies the macro arrays to host, ghosted scalar layout; any pointer may be
+ * NULL (src/dugks.cu:393-405 copy_vel). */
+int dg_copy_vel(dg_t *h, double *rho, double *ux, double *uy, double *uz);
+
+/* diag.dat values (mean rho,u,v,w; min ...; max ...) and the 9 x nx
+ * profiles-2.dat values of src/output.cu:223-334, reduced on the device in
+ * FP64 from the current state (calls dg_upload_macro). */
+int dg_stats_values(dg_t *h, double *diag12, double *prof9);
+
+/* Appends diag.dat and profiles-2.dat in the working directory with the
+ * reference's formats (src/output.cu:261-333). */
+int dg_stats(dg_t *h, int step);
+
+/* dg_stats plus the Tecplot slices s2X/s2Y/s2Z%08d.tec of
+ * src/output.cu:152-218 (output_2d, src/output.cu:118-147). */
+int dg_output_2d(dg_t *h, int step);
+
+/* --- state and checkpoint I/O ------------------------------------------ */
+
+/* Full ghosted AoS copy of f-tilde (src/dugks.cu:407-416 copy_ddf); ghost
+ * entries are written as 0. */
+int dg_copy_ddf(dg_t *h, double *f_ghosted);
+
+/* Interior state in dump order (get) / load it (set). */
+int dg_get_state(dg_t *h, double *f_dump_order);
+int dg_set_state(dg_t *h, const double *f_dump_order);
+
+/* ddf%08d.dat in the working directory: raw native-endian reals of the
+ * engine's dump width (8 B for fp64, 4 B otherwise), dump order, no header
+ * (src/output.cu:22-89). */
+int dg_dump(dg_t *h, int step);
+int dg_read_dump(dg_t *h, int step);
+
+/* Read-only device pointer of one of the DG_BUF_* buffers. */
+const void *dg_device_ptr(const dg_t *h, int which);
+
+/* --- harness hooks (used by the adjoint verification harness) ---------- */
+
+/* Total mass, x/y/z momentum of the current state in FP64. */
+int dg_moments(dg_t *h, double *mass_mom4);
+
+/* Cell centres and widths along x, nx+2 entries each (index 0 and nx+1 are
+ * the mirrored ghosts of src/fortran/channel/src/dugks.cuf:118-121); either
+ * pointer may be NULL. */
+int dg_get_mesh(const dg_t *h, double *xc, double *dxx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
