@@ -126,6 +126,18 @@ def ncu_traffic(precision):
         return None
 
 
+def combine_ranks(world, n_cells, steps, ms_local, dist=None, device="cpu"):
+    """Whole-job MLUPS of `world` replicas: every rank advanced n_cells for
+    `steps` steps; the job time is the maximum over ranks."""
+    ms = float(ms_local)
+    if dist is not None and world > 1:
+        import torch
+        t = torch.tensor([ms], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return world * n_cells * steps / (ms / 1e3) / 1e6, ms
+
+
 def time_steps(eng, istep0, k):
     import torch
     e0 = torch.cuda.Event(enable_timing=True)
@@ -273,11 +285,7 @@ def main():
     time.sleep(0.3)
     ms, ms_a, ms_b = time_steps(eng, W + 1, K)
     clocks = sampler.stop()
-    if dist:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n * K / (ms / 1e3) / 1e6
+    value, ms = combine_ranks(world, n, K, ms, dist, device="cuda")
 
     # end to end through the C ABI with host buffers: upload the state from
     # pinned host memory, K steps each followed by a host read of the step's

@@ -1,0 +1,416 @@
+// Hand-written adjoint (transposed Jacobian) of one DUGKS step.
+//
+// The forward step S (dugks_kernels.cuh) is
+//   fb   = A(f)                         stage (a), per cell
+//   v    = L(G fb)                      ghost formation G, interpolation L (linear)
+//   v'   = B v                          bounce-back on the wall faces (linear)
+//   F    = phi(v')                      face equilibrium + flux, per face
+//   f'   = 4/3 fb - 1/3 f - D F         finite-volume update (linear)
+// Given lam' = dJ/df', the adjoint step returns lam = (dS/df)^T lam':
+//   lamF = -D^T lam'                    (per face, the two adjacent cells)
+//   lamv = B^T (dphi/dv')^T lamF        adj_face_kernel, one thread per face
+//   mu   = 4/3 lam' + G^T L^T lamv      adj_gather_kernel (gather form, deterministic)
+//   lam  = (dA/df)^T mu - 1/3 lam'      adj_gather_kernel
+// For a face or a cell with density r, first moment j, u0 = j/r,
+// u = u0 + shift, coefficient c_p = fw2 + 3 fw0 (F.c_p - F.u) and
+// feq_p = w_p r (1 + 3 c_p.u + 4.5 (c_p.u)^2 - 1.5 u.u), the map
+// out_p = w1 x_p + c_p feq_p has the transposed Jacobian
+//   lam_x_q = w1 lamo_q + (S0 + G.(c_q - u0)) / r
+//   S0 = sum_p lamo_p c_p feq_p
+//   G  = sum_p lamo_p [c_p w_p r (3 c_p + 9 (c_p.u) c_p - 3 u) - 3 w0 F feq_p].
+#pragma once
+#include "dugks_kernels.cuh"
+
+namespace dg {
+
+template <class T>
+struct AdjJac {
+    T S0, G[3];
+};
+
+// Accumulate one population's term of S0 and G; lam is the adjoint of
+// out_p = w1 x_p + coef_p feq_p with coef_p = cb + Kp (cb = w2 - 3 w0 F.u).
+template <class T>
+__device__ __forceinline__ void adj_accum(AdjJac<T> &J, int p, T lam, T r, T u, T v, T w, T coef, T feq,
+                                          T w0x3, const T F[3])
+{
+    const T cu = T(cx(p)) * u + T(cy(p)) * v + T(cz(p)) * w;
+    const T a = lam * coef * weight<T>(p) * r;
+    const T b = T(3) + T(9) * cu;
+    J.S0 += lam * coef * feq;
+    const T lf = lam * feq * w0x3;
+    J.G[0] += a * (b * T(cx(p)) - T(3) * u) - lf * F[0];
+    J.G[1] += a * (b * T(cy(p)) - T(3) * v) - lf * F[1];
+    J.G[2] += a * (b * T(cz(p)) - T(3) * w) - lf * F[2];
+}
+
+template <class T, class S>
+__device__ __forceinline__ T fb_at(const S *fb, const StepParams<T, S> &P, int p, int gi, int gj, int gk)
+{
+    // gi, gj, gk: 1-based with ghosts 0 / n+1 (periodic wrap or wall extrapolation in x)
+    gj = gj == 0 ? P.ny : (gj == P.ny + 1 ? 1 : gj);
+    gk = gk == 0 ? P.nz : (gk == P.nz + 1 ? 1 : gk);
+    const long long row = ((long long)(gk - 1) * P.ny + (gj - 1)) * P.pitch;
+    if (gi == 0 || gi == P.nx + 1) {
+        if (P.periodic_x) {
+            gi = gi == 0 ? P.nx : 1;
+        } else {
+            const int a = gi == 0 ? 1 : P.nx, b = gi == 0 ? 2 : P.nx - 1;
+            const T q = gi == 0 ? P.q0 : P.q1;
+            const T fa = P.codec.load_nc(fb, p * P.ps + row + (a - 1), p);
+            const T fbv = P.codec.load_nc(fb, p * P.ps + row + (b - 1), p);
+            return q * fa + (T(1) - q) * fbv;
+        }
+    }
+    return P.codec.load_nc(fb, p * P.ps + row + (gi - 1), p);
+}
+
+template <class T, class S>
+__device__ __forceinline__ T lam_at(const S *lam, const StepParams<T, S> &P, int p, int gi, int gj, int gk)
+{
+    const long long c = ((long long)(gk - 1) * P.ny + (gj - 1)) * P.pitch + (gi - 1);
+    return T(lam[p * P.ps + c]);
+}
+
+// Number of faces of each orientation in the per-face adjoint buffers.
+//   x faces: I = 0..nx (face I between cells I and I+1), per (j, k)
+//   y faces: J = 1..ny (between J and J+1, periodic), per (i, k)
+//   z faces: K = 1..nz, per (i, j)
+__host__ __device__ inline long long adj_nface(int ax, int nx, int ny, int nz)
+{
+    return ax == 0 ? (long long)(nx + 1) * ny * nz : (long long)nx * ny * nz;
+}
+__host__ __device__ inline long long adj_xface(int I, int j, int k, int nx, int ny)
+{
+    return ((long long)(k - 1) * ny + (j - 1)) * (nx + 1) + I;
+}
+__host__ __device__ inline long long adj_cell(int i, int j, int k, int nx, int ny)
+{
+    return ((long long)(k - 1) * ny + (j - 1)) * nx + (i - 1);
+}
+
+// Per-face adjoint: reconstruct the face values, take the flux adjoint from
+// the two adjacent cells' lam', apply (dphi/dv)^T and the bounce-back
+// transpose, store lamv[19] of the face (population-major, stride nface).
+template <class T, class S, int AX>
+__global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb, const S *__restrict__ lam_next,
+                                                       T *__restrict__ lamv, const StepParams<T, S> P)
+{
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const long long nface = adj_nface(AX, nx, ny, nz);
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nface) return;
+    int I = 0, i = 1, j, k;
+    if (AX == 0) {
+        I = int(q % (nx + 1));
+        const long long r = q / (nx + 1);
+        j = int(r % ny) + 1;
+        k = int(r / ny) + 1;
+        if (P.periodic_x && I == 0) {
+            for (int p = 0; p < NPOP; ++p) lamv[p * nface + q] = T(0);  // periodic: face 0 is face nx
+            return;
+        }
+    } else {
+        i = int(q % nx) + 1;
+        const long long r = q / nx;
+        j = int(r % ny) + 1;
+        k = int(r / ny) + 1;
+    }
+    // --- face values (same interpolation as face_values, global loads) ---
+    T v[NPOP];
+    int A = i, Bc = i;  // x faces: anchor and other column
+    const T *xwf = nullptr;
+    if (AX == 0) {
+        A = I == 0 ? 1 : I;
+        Bc = I == 0 ? 0 : I + 1;
+        xwf = P.xw + (size_t)I * 38;
+    }
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) {
+        const int ax = cx(p), ay = cy(p), az = cz(p);
+        if (p == 0) {
+            T a, b;
+            if (AX == 0) { a = fb_at(fb, P, 0, A, j, k); b = fb_at(fb, P, 0, Bc, j, k); }
+            else if (AX == 1) { a = fb_at(fb, P, 0, i, j, k); b = fb_at(fb, P, 0, i, j + 1, k); }
+            else { a = fb_at(fb, P, 0, i, j, k); b = fb_at(fb, P, 0, i, j, k + 1); }
+            v[0] = T(0.5) * (a + b);
+            continue;
+        }
+        if (AX == 0) {
+            const T om = __ldg(xwf + 2 * p), m = __ldg(xwf + 2 * p + 1);
+            auto xl = [&](int jj, int kk) { return lerp2(om, m, fb_at(fb, P, p, A, jj, kk), fb_at(fb, P, p, Bc, jj, kk)); };
+            const T x00 = xl(j, k);
+            T y00 = x00;
+            if (ay) y00 = lerp2(P.ty_om, P.ty_m, x00, xl(j - ay, k));
+            if (az) {
+                const T x10 = xl(j, k - az);
+                T y11 = x10;
+                if (ay) y11 = lerp2(P.ty_om, P.ty_m, x10, xl(j - ay, k - az));
+                v[p] = lerp2(P.tz_om, P.tz_m, y00, y11);
+            } else {
+                v[p] = y00;
+            }
+        } else {
+            T txo = T(1), txm = T(0);
+            if (ax) {
+                txo = __ldg(P.txw + (size_t)i * 38 + 2 * p);
+                txm = __ldg(P.txw + (size_t)i * 38 + 2 * p + 1);
+            }
+            auto xt = [&](int jj, int kk) {
+                T a = fb_at(fb, P, p, i, jj, kk);
+                if (ax) a = lerp2(txo, txm, a, fb_at(fb, P, p, i - ax, jj, kk));
+                return a;
+            };
+            if (AX == 1) {
+                const T y00 = lerp2(P.yn_om[p], P.yn_m[p], xt(j, k), xt(j + 1, k));
+                if (az) {
+                    const T y11 = lerp2(P.yn_om[p], P.yn_m[p], xt(j, k - az), xt(j + 1, k - az));
+                    v[p] = lerp2(P.tz_om, P.tz_m, y00, y11);
+                } else {
+                    v[p] = y00;
+                }
+            } else {
+                T y00 = xt(j, k), y11 = xt(j, k + 1);
+                if (ay) {
+                    y00 = lerp2(P.ty_om, P.ty_m, y00, xt(j - ay, k));
+                    y11 = lerp2(P.ty_om, P.ty_m, y11, xt(j - ay, k + 1));
+                }
+                v[p] = lerp2(P.zn_om[p], P.zn_m[p], y00, y11);
+            }
+        }
+    }
+    const bool lo = AX == 0 && !P.periodic_x && I == 0;
+    const bool hi = AX == 0 && !P.periodic_x && I == nx;
+    bounce_back(v, lo, hi);
+
+    // --- lamF of the 10 crossing populations from the adjacent cells ---
+    T lamF[NPOP];
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) lamF[p] = T(0);
+    if (AX == 0) {
+        const int L = I, R = I + 1 <= nx ? I + 1 : (P.periodic_x ? 1 : 0);
+        const T cl = L >= 1 ? __ldg(P.cxu + L) : T(0);
+        const T cr = R >= 1 ? __ldg(P.cxu + R) : T(0);
+#pragma unroll
+        for (int s = 0; s < 10; ++s) {
+            const int p = flux_pop(0, s);
+            T a = T(0);
+            if (R >= 1) a += cr * lam_at(lam_next, P, p, R, j, k);
+            if (L >= 1) a -= cl * lam_at(lam_next, P, p, L, j, k);
+            lamF[p] = T(cx(p)) * a;
+        }
+    } else if (AX == 1) {
+        const int J2 = j + 1 <= ny ? j + 1 : 1;
+#pragma unroll
+        for (int s = 0; s < 10; ++s) {
+            const int p = flux_pop(1, s);
+            lamF[p] = T(cy(p)) * P.cyu * (lam_at(lam_next, P, p, i, J2, k) - lam_at(lam_next, P, p, i, j, k));
+        }
+    } else {
+        const int K2 = k + 1 <= nz ? k + 1 : 1;
+#pragma unroll
+        for (int s = 0; s < 10; ++s) {
+            const int p = flux_pop(2, s);
+            lamF[p] = T(cz(p)) * P.czu * (lam_at(lam_next, P, p, i, j, K2) - lam_at(lam_next, P, p, i, j, k));
+        }
+    }
+
+    // --- (dphi/dv)^T ---
+    T r, jx, jy, jz;
+    moments(v, r, jx, jy, jz);
+    const T inv = T(1) / r;
+    const T u0 = jx * inv, v0 = jy * inv, w0 = jz * inv;
+    T u = u0, vv = v0, w = w0, B = P.fw2;
+    if (P.force_on) {
+        u += P.hF[0];
+        vv += P.hF[1];
+        w += P.hF[2];
+        B = fma(-P.fw0x3, fma(P.F[0], u, fma(P.F[1], vv, P.F[2] * w)), P.fw2);
+    }
+    T fe[NPOP];
+    feq_all(r, u, vv, w, fe);
+    AdjJac<T> Jc = {T(0), {T(0), T(0), T(0)}};
+#pragma unroll
+    for (int s = 0; s < 10; ++s) {
+        const int p = flux_pop(AX, s);
+        adj_accum(Jc, p, lamF[p], r, u, vv, w, B + P.Kf[p], fe[p], P.fw0x3, P.F);
+    }
+    T lv[NPOP];
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) {
+        const T g = Jc.S0 + Jc.G[0] * (T(cx(p)) - u0) + Jc.G[1] * (T(cy(p)) - v0) + Jc.G[2] * (T(cz(p)) - w0);
+        lv[p] = P.fw1 * lamF[p] + g * inv;
+    }
+    // bounce-back transpose
+    if (lo) {
+        lv[2] += lv[1]; lv[1] = T(0); lv[10] += lv[7]; lv[7] = T(0); lv[8] += lv[9]; lv[9] = T(0);
+        lv[14] += lv[11]; lv[11] = T(0); lv[12] += lv[13]; lv[13] = T(0);
+    }
+    if (hi) {
+        lv[1] += lv[2]; lv[2] = T(0); lv[7] += lv[10]; lv[10] = T(0); lv[9] += lv[8]; lv[8] = T(0);
+        lv[11] += lv[14]; lv[14] = T(0); lv[13] += lv[12]; lv[12] = T(0);
+    }
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) lamv[p * nface + q] = lv[p];
+}
+
+// Adjoint received by the f-bar-plus value of population p at column gi
+// (0..nx+1, ghosts included) of row j, plane k, through the interpolation of
+// every face whose stencil contains it (the transpose of L).
+template <class T, class S>
+__device__ __forceinline__ T adj_received(const T *__restrict__ LX, const T *__restrict__ LY,
+                                          const T *__restrict__ LZ, const StepParams<T, S> &P, int p, int gi,
+                                          int j, int k)
+{
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const int ax = cx(p), ay = cy(p), az = cz(p);
+    const long long nfx = adj_nface(0, nx, ny, nz), nfc = adj_nface(1, nx, ny, nz);
+    auto wrapj = [&](int jj) { return jj < 1 ? jj + ny : (jj > ny ? jj - ny : jj); };
+    auto wrapk = [&](int kk) { return kk < 1 ? kk + nz : (kk > nz ? kk - nz : kk); };
+    auto wrapi = [&](int ii) { return ii < 1 ? ii + nx : (ii > nx ? ii - nx : ii); };
+    T acc = T(0);
+    // transverse weights (1-t at the face's own row/plane, t at the shifted one)
+    const T tyo = p == 0 ? T(1) : P.ty_om, tym = P.ty_m, tzo = p == 0 ? T(1) : P.tz_om, tzm = P.tz_m;
+
+    // ---- x faces: anchor / other columns ----
+    {
+        auto xsum = [&](int I, T wx) {
+            // rows j' with j = j' (1-ty) or j = j'+cy (ty); planes likewise
+            T s = T(0);
+            const T *base = LX + (long long)p * nfx;
+            s += (ay ? tyo : T(1)) * (az ? tzo : T(1)) * base[adj_xface(I, j, k, nx, ny)];
+            if (ay) s += tym * (az ? tzo : T(1)) * base[adj_xface(I, wrapj(j + ay), k, nx, ny)];
+            if (az) s += (ay ? tyo : T(1)) * tzm * base[adj_xface(I, j, wrapk(k + az), nx, ny)];
+            if (ay && az) s += tym * tzm * base[adj_xface(I, wrapj(j + ay), wrapk(k + az), nx, ny)];
+            return wx * s;
+        };
+        auto xw = [&](int I, int which) -> T {
+            if (p == 0) return T(0.5);
+            return __ldg(P.xw + (size_t)I * 38 + 2 * p + which);
+        };
+        if (P.periodic_x) {
+            // faces I = 1..nx, anchor I, other I+1 (nx+1 -> 1)
+            if (gi >= 1 && gi <= nx) {
+                acc += xsum(gi, xw(gi, 0));
+                const int Io = gi == 1 ? nx : gi - 1;
+                acc += xsum(Io, xw(Io, 1));
+            }
+        } else {
+            if (gi >= 1 && gi <= nx) acc += xsum(gi, xw(gi, 0));      // anchor of face gi
+            if (gi == 1) acc += xsum(0, xw(0, 0));                    // anchor of face 0
+            if (gi >= 2 && gi <= nx + 1) acc += xsum(gi - 1, xw(gi - 1, 1));  // other of face gi-1
+            if (gi == 0) acc += xsum(0, xw(0, 1));                    // other of face 0
+        }
+    }
+    // ---- y and z faces: column i with weight (1-tx(i)) if i = gi, tx(i) if i - cx = gi ----
+    auto colw = [&](int i, int self) -> T {
+        if (!ax) return self ? T(1) : T(0);
+        return __ldg(P.txw + (size_t)i * 38 + 2 * p + (self ? 0 : 1));
+    };
+    int cols[2];
+    T cw[2];
+    int nc = 0;
+    if (gi >= 1 && gi <= nx) { cols[nc] = gi; cw[nc] = colw(gi, 1); ++nc; }
+    if (ax) {
+        int i2 = gi + ax;
+        if (P.periodic_x) i2 = wrapi(i2);
+        if (i2 >= 1 && i2 <= nx && !(P.periodic_x && (gi < 1 || gi > nx))) { cols[nc] = i2; cw[nc] = colw(i2, 0); ++nc; }
+    }
+    for (int c = 0; c < nc; ++c) {
+        const int i = cols[c];
+        const T wc = cw[c];
+        // y faces J (anchor row J = j, other row J+1 = j -> J = j-1)
+        {
+            const T *base = LY + (long long)p * nfc;
+            const T yo = p == 0 ? T(0.5) : P.yn_om[p], ym = p == 0 ? T(0.5) : P.yn_m[p];
+            T s = yo * base[adj_cell(i, j, k, nx, ny)] + ym * base[adj_cell(i, wrapj(j - 1), k, nx, ny)];
+            if (az) {
+                s = (p == 0 ? T(1) : tzo) * s;
+                s += tzm * (yo * base[adj_cell(i, j, wrapk(k + az), nx, ny)] +
+                            ym * base[adj_cell(i, wrapj(j - 1), wrapk(k + az), nx, ny)]);
+            }
+            acc += wc * s;
+        }
+        // z faces K (anchor plane K = k, other plane K+1 = k -> K = k-1)
+        {
+            const T *base = LZ + (long long)p * nfc;
+            const T zo = p == 0 ? T(0.5) : P.zn_om[p], zm = p == 0 ? T(0.5) : P.zn_m[p];
+            T s = zo * base[adj_cell(i, j, k, nx, ny)] + zm * base[adj_cell(i, j, wrapk(k - 1), nx, ny)];
+            if (ay) {
+                s = tyo * s;
+                s += tym * (zo * base[adj_cell(i, wrapj(j + ay), k, nx, ny)] +
+                            zm * base[adj_cell(i, wrapj(j + ay), wrapk(k - 1), nx, ny)]);
+            }
+            acc += wc * s;
+        }
+    }
+    return acc;
+}
+
+// mu = 4/3 lam' + (G^T L^T lamv); lam = (dA/df)^T mu - 1/3 lam'.
+template <class T, class S>
+__global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f, const S *__restrict__ lam_next,
+                                                         const T *__restrict__ LX, const T *__restrict__ LY,
+                                                         const T *__restrict__ LZ, S *__restrict__ lam_out,
+                                                         const StepParams<T, S> P)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y + 1, k = blockIdx.z + 1;
+    if (i > P.nx) return;
+    const long long c = ((long long)(k - 1) * P.ny + (j - 1)) * P.pitch + (i - 1);
+    T mu[NPOP];
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) {
+        T m = T(4.0 / 3.0) * T(lam_next[p * P.ps + c]) + adj_received(LX, LY, LZ, P, p, i, j, k);
+        if (!P.periodic_x) {
+            // wall ghosts: g0 = q0 fb1 + (1-q0) fb2, g_{nx+1} = q1 fb_nx + (1-q1) fb_{nx-1}
+            if (i == 1) m += P.q0 * adj_received(LX, LY, LZ, P, p, 0, j, k);
+            if (i == 2) m += (T(1) - P.q0) * adj_received(LX, LY, LZ, P, p, 0, j, k);
+            if (i == P.nx) m += P.q1 * adj_received(LX, LY, LZ, P, p, P.nx + 1, j, k);
+            if (i == P.nx - 1) m += (T(1) - P.q1) * adj_received(LX, LY, LZ, P, p, P.nx + 1, j, k);
+        }
+        mu[p] = m;
+    }
+    // stage (a) transpose at this cell
+    T v[NPOP];
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) v[p] = T(f[p * P.ps + c]);
+    T r, jx, jy, jz;
+    moments(v, r, jx, jy, jz);
+    const T inv = T(1) / r;
+    const T u0 = jx * inv, v0 = jy * inv, w0 = jz * inv;
+    T Fx, Fy, Fz;
+    cell_force(P, i - 1, j - 1, k - 1, Fx, Fy, Fz);
+    const T Fc[3] = {Fx, Fy, Fz};
+    const bool forced = P.force_on || P.perturb;
+    T u = u0, vv = v0, w = w0, B = P.bw2;
+    if (forced) {
+        u = fma(P.hdt, Fx, u);
+        vv = fma(P.hdt, Fy, vv);
+        w = fma(P.hdt, Fz, w);
+        B = fma(-P.bw0x3, fma(Fx, u, fma(Fy, vv, Fz * w)), P.bw2);
+    }
+    T fe[NPOP];
+    feq_all(r, u, vv, w, fe);
+    AdjJac<T> Jc = {T(0), {T(0), T(0), T(0)}};
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) {
+        T K = P.Kb[p];
+        if (P.perturb) {
+            T cf = T(0);
+            if (cx(p)) cf += cx(p) > 0 ? Fx : -Fx;
+            if (cy(p)) cf += cy(p) > 0 ? Fy : -Fy;
+            if (cz(p)) cf += cz(p) > 0 ? Fz : -Fz;
+            K = P.bw0x3 * cf;
+        }
+        adj_accum(Jc, p, mu[p], r, u, vv, w, B + K, fe[p], P.bw0x3, Fc);
+    }
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) {
+        const T g = Jc.S0 + Jc.G[0] * (T(cx(p)) - u0) + Jc.G[1] * (T(cy(p)) - v0) + Jc.G[2] * (T(cz(p)) - w0);
+        const T out = P.bw1 * mu[p] + g * inv - T(1.0 / 3.0) * T(lam_next[p * P.ps + c]);
+        lam_out[p * P.ps + c] = S(out);
+    }
+}
+
+}  // namespace dg
