@@ -47,22 +47,11 @@ __device__ __forceinline__ void adj_accum(AdjJac<T> &J, int p, T lam, T r, T u, 
 template <class T, class S>
 __device__ __forceinline__ T fb_at(const S *fb, const StepParams<T, S> &P, int p, int gi, int gj, int gk)
 {
-    // gi, gj, gk: 1-based with ghosts 0 / n+1 (periodic wrap or wall extrapolation in x)
+    // gi: stored column 0..nx+1 (x ghosts held by fb_ghost_kernel); gj, gk 1-based with periodic wrap
     gj = gj == 0 ? P.ny : (gj == P.ny + 1 ? 1 : gj);
     gk = gk == 0 ? P.nz : (gk == P.nz + 1 ? 1 : gk);
-    const long long row = ((long long)(gk - 1) * P.ny + (gj - 1)) * P.pitch;
-    if (gi == 0 || gi == P.nx + 1) {
-        if (P.periodic_x) {
-            gi = gi == 0 ? P.nx : 1;
-        } else {
-            const int a = gi == 0 ? 1 : P.nx, b = gi == 0 ? 2 : P.nx - 1;
-            const T q = gi == 0 ? P.q0 : P.q1;
-            const T fa = P.codec.load_nc(fb, p * P.ps + row + (a - 1), p);
-            const T fbv = P.codec.load_nc(fb, p * P.ps + row + (b - 1), p);
-            return q * fa + (T(1) - q) * fbv;
-        }
-    }
-    return P.codec.load_nc(fb, p * P.ps + row + (gi - 1), p);
+    const long long row = ((long long)(gk - 1) * P.ny + (gj - 1)) * P.pitch_b;
+    return P.codec.load_nc(fb, p * P.ps_b + row + gi, p);
 }
 
 template <class T, class S>

@@ -80,6 +80,8 @@ __global__ void __launch_bounds__(1024) stats_partials_kernel(const S *__restric
 
 // Ordered reduction over blocks: total[i][s] = sum/min/max over b of partial[b][i][s].
 __global__ void stats_reduce_kernel(const double *__restrict__ partial, int nblocks, int nx, double *__restrict__ total);
+// acc[i][s] += total[i][s] for the 10 sums
+__global__ void stats_accumulate_kernel(const double *__restrict__ total, int nx, double *__restrict__ acc);
 
 // Conserved moments: block partial sums of (rho, jx, jy, jz) over cells.
 template <class T, class S>

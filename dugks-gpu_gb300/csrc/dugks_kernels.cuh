@@ -1,16 +1,19 @@
 // DUGKS D3Q19 step kernels for sm_103a.
 //
-// Layout in HBM: structure of arrays, interior cells only, one plane per
-// population: a[p*ps + ((k*ny + j)*pitch + i)] (0-based i, j, k).  There is no
-// ghost layer: the periodic images and the wall extrapolation of f-bar-plus
-// are formed while the flux kernel stages a tile in shared memory, which
-// replaces the reference's extend_fb_x / extend_fb_x_wall / extend_fb_y
-// kernels and the MPI z exchange (src/dugks.cu:348-377, src/parallel.cu:185-234).
+// Layout in HBM: structure of arrays, one plane per population.
+//   f-tilde:         f[p*ps + ((k*ny + j)*pitch + i)]           (0-based i, j, k; interior only)
+//   f-bar-plus:     fb[p*ps_b + ((k*ny + j)*pitch_b + i + 1)]   (x ghost columns at 0 and nx+1)
+// The x ghosts of f-bar-plus are stored by fb_ghost_kernel; the y and z
+// periodic images are index wraps in the flux kernel.  Together they replace
+// the reference's extend_fb_x / extend_fb_x_wall / extend_fb_y kernels and
+// the MPI z exchange (src/dugks.cu:348-377, src/parallel.cu:185-234).
 //
 // Kernels:
 //   fbar_kernel      stage (a), src/dugks.cu:1131-1196 (calc_fb1)
-//   flux_kernel      stages (c) (d) (e), src/dugks.cu:715-959 (calc_fx_tri),
-//                    each face evaluated once, z-marching tile in shared memory
+//   fb_ghost_kernel  x ghost columns of f-bar-plus (periodic images / wall extrapolation)
+//   flux_kernel      stages (c) (d) (e), src/dugks.cu:715-959 (calc_fx_tri) or the
+//                    central-difference variant 421-649 (calc_fx); every face
+//                    evaluated once, z-marching warp rows
 //   macro_kernel     src/dugks.cu:1021-1064 (calc_macro)
 //
 // Template parameters: T is the arithmetic type, S the storage type of f and
@@ -31,7 +34,9 @@ namespace dg {
 template <class T, class S>
 struct StepParams {
     int nx, ny, nz, pitch;
-    long long ps;          // population stride (elements)
+    long long ps;          // population stride of f-tilde (elements)
+    int pitch_b;           // x pitch of f-bar-plus, which stores the ghost columns 0 and nx+1
+    long long ps_b;        // population stride of f-bar-plus
     int periodic_x;        // 0: bounce-back walls on the two x faces
     int perturb;           // per-cell perturbation force in stage (a)
     int force_on;          // ambient force non-zero
@@ -50,6 +55,8 @@ struct StepParams {
     T zn_om[NPOP], zn_m[NPOP];   // z-face normal (dz/2 - hdt*cz)/dz
     T cyu, czu;                  // dt/dy, dt/dz
     T q0, q1;                    // wall ghost extrapolation weights (2 on a uniform mesh)
+    T g_idx, g_idy, g_idz;       // gradient reconstruction: 1/dx, 1/dy, 1/dz
+    T g_i2dx, g_i2dy, g_i2dz;    // 1/(2dx), 1/(2dy), 1/(2dz)
     const T *xw;                 // [(nx+1)*19*2] x-face normal (1-m, m); face I lies between cells I, I+1 (1-based)
     const T *txw;                // [(nx+2)*19*2] transverse x (1-t, t) per column 0..nx+1
     const T *cxu;                // [nx+2] dt/dxx(i)
@@ -145,6 +152,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     const int k = blockIdx.z;
     if (i >= P.nx) return;
     const long long c = ((long long)k * P.ny + j) * P.pitch + i;
+    const long long cb = ((long long)k * P.ny + j) * P.pitch_b + i + 1;
 
     T v[NPOP];
 #pragma unroll
@@ -181,126 +189,171 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
             K = P.bw0x3 * cf;
         }
         const T out = fma(B + K, fe[p], P.bw1 * v[p]);
-        P.codec.store(fb, p * P.ps + c, p, out);
+        P.codec.store(fb, p * P.ps_b + cb, p, out);
     }
 }
 
 // ---------------------------------------------------------------------------
-// Stages (c) (d) (e): face reconstruction, face flux, finite-volume update.
-//
-// One CTA owns a BX x BY column of cells and marches over a chunk of z
-// planes.  Three planes of f-bar-plus (k-1, k, k+1) with a one-cell halo in x
-// and y live in shared memory; every face of plane k is reconstructed once:
-//   x faces I-1/2 .. I+BX-1/2 of each row, y faces likewise, z face k+1/2;
-// the 10 fluxes of each face (populations with c_normal != 0) go to shared
-// memory and the cells of plane k are updated from them.
+// Ghost columns of f-bar-plus (i = 0 and nx+1 of the 1-based x index): the
+// periodic images (src/dugks.cu:1212-1229) or the linear wall extrapolation
+// (src/dugks.cu:1234-1251; stretched mesh src/fortran/channel/src/dugks.cuf:365-374).
+// The y and z images are formed by index wrapping in the flux kernel, which
+// together replaces extend_fb_y and the z halo exchange.
 // ---------------------------------------------------------------------------
-template <class T, int BX, int BY>
-struct FluxTile {
-    static constexpr int PW = BX + 2, PH = BY + 2, PL = PW * PH;
-    static constexpr int NXF = (BX + 1) * BY, NYF = BX * (BY + 1), NZF = BX * BY;
-    static constexpr int pad32(int n) { return (n + 31) / 32 * 32; }
-    static constexpr int NXFP = pad32(NXF), NYFP = pad32(NYF), NZFP = pad32(NZF);
-    static constexpr size_t elems = 3 * NPOP * PL + 10 * (NXF + NYF + 2 * NZF);
-    static constexpr size_t bytes = sizeof(T) * elems;
-};
-
-// Reconstruct the 19 values of one face from the staged planes and return the
-// 10 fluxes of the populations crossing it.
-//   AX = 0: x face between anchor column sa and other column sa+dxo (row sj)
-//   AX = 1: y face between anchor row and the row above
-//   AX = 2: z face between plane k (anchor) and plane k+1
-// `pA` / `pB`: planes holding the anchor / other side along the normal for
-// AX=2; for AX=0,1 pA is plane k, and pM / pP are planes k-1 / k+1 used by
-// the transverse z shift (c_z = +1 reads plane k-1).
-template <class T, class S, int AX, int BX, int BY>
-__device__ __forceinline__ void face_values(const StepParams<T, S> &P, const T *pA, const T *pB, const T *pM, const T *pP,
-                                            int sa, int dxo, int gi, const T *xw_face, T v[NPOP])
+template <class T, class S>
+__global__ void __launch_bounds__(256) fb_ghost_kernel(S *__restrict__ fb, const StepParams<T, S> P)
 {
-    using Tile = FluxTile<T, BX, BY>;
-    constexpr int PW = Tile::PW, PL = Tile::PL;
+    const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (k*ny + j)
+    if (row >= (long long)P.ny * P.nz) return;
+    const long long base = row * P.pitch_b;
+    const int nx = P.nx;
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
-        const T *base = pA + p * PL;
-        if (p == 0) {
-            // rest population: mean of the two cells across the face (src/dugks.cu:756-763)
-            const int o = AX == 0 ? dxo : (AX == 1 ? PW : 0);
-            const T a = base[sa];
-            const T b = AX == 2 ? pB[sa] : base[sa + o];
-            v[0] = T(0.5) * (a + b);
-            continue;
+        S *r = fb + p * P.ps_b + base;
+        if (P.periodic_x) {
+            r[0] = r[nx];
+            r[nx + 1] = r[1];
+        } else {
+            const T a0 = P.codec.load(r, 1, p), a1 = P.codec.load(r, 2, p);
+            const T b0 = P.codec.load(r, nx, p), b1 = P.codec.load(r, nx - 1, p);
+            P.codec.store(r, 0, p, P.q0 * a0 + (T(1) - P.q0) * a1);
+            P.codec.store(r, nx + 1, p, P.q1 * b0 + (T(1) - P.q1) * b1);
         }
-        const int ax = cx(p), ay = cy(p), az = cz(p);
-        if (AX == 0) {
-            // x normal; y shift jj=-cy; z shift kk=-cz (plane k-cz)
-            const T om = __ldg(xw_face + 2 * p), m = __ldg(xw_face + 2 * p + 1);
-            const int jo = -ay * PW;
-            const T *b0 = base;
-            const T *b1 = az > 0 ? pM + p * PL : (az < 0 ? pP + p * PL : base);
-            const T x00 = lerp2(om, m, b0[sa], b0[sa + dxo]);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Stages (b)/(c), (d), (e): face reconstruction, face flux, finite-volume update.
+//
+// A CTA is W warps.  Warps 1..W-1 each own one row of 32 cells (lane = x)
+// and march over a chunk of z planes; per plane every thread evaluates the
+// +x, +y and +z faces of its cell once, takes the -x face from lane-1
+// (warp shuffle), the -y face from the warp below (shared memory) and the
+// -z face from its own previous plane (register), and updates its cell.
+// Warp 0 is the halo: it evaluates the -y faces of the first row and, one
+// lane per row, the -x faces of the first column.  f-bar-plus is read through
+// L1 (no shared-memory staging); its ghost columns are stored by
+// fb_ghost_kernel and its y / z images are index wraps.
+// ---------------------------------------------------------------------------
+template <class T, class S>
+struct FbRead {
+    const S *fb;
+    long long ps;
+    int pitch, ny, nz;
+    const Codec<T, S> &codec;
+    __device__ __forceinline__ long long rb(int j, int k) const
+    {
+        return ((long long)(k - 1) * ny + (j - 1)) * pitch;
+    }
+    __device__ __forceinline__ T operator()(int p, long long row, int col) const
+    {
+        return codec.load_nc(fb, p * ps + row + col, p);
+    }
+};
+
+__device__ __forceinline__ int wrap1(int j, int n)
+{
+    // 1-based periodic index for j in [0, 2n]; values beyond clamp (unused lanes)
+    j = j < 1 ? j + n : (j > n ? j - n : j);
+    return j < 1 ? 1 : (j > n ? n : j);
+}
+
+// 19 reconstructed values of one face, trilinear characteristic interpolation
+// (src/dugks.cu:756-906) in the reference's x -> y -> z lerp order:
+//   AX=0: face I between columns I and I+1 (I = 0: anchor column 1, other 0)
+//   AX=1: face J between rows J and J+1 at column i
+//   AX=2: face K between planes K and K+1 at column i
+template <class T, class S, int AX>
+__device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const FbRead<T, S> &R, int i, int j, int k,
+                                         T v[NPOP])
+{
+    const int ny = P.ny, nz = P.nz;
+    const int jm = wrap1(j - 1, ny), jp = wrap1(j + 1, ny), jc = wrap1(j, ny);
+    const int km = wrap1(k - 1, nz), kp = wrap1(k + 1, nz), kc = wrap1(k, nz);
+    if (AX == 0) {
+        const int A = i == 0 ? 1 : i, B = i == 0 ? 0 : i + 1;
+        const T *xw = P.xw + (size_t)i * 38;
+        const long long r00 = R.rb(jc, kc);
+        v[0] = T(0.5) * (R(0, r00, A) + R(0, r00, B));
+#pragma unroll
+        for (int p = 1; p < NPOP; ++p) {
+            const int ay = cy(p), az = cz(p);
+            const T om = __ldg(xw + 2 * p), m = __ldg(xw + 2 * p + 1);
+            const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
+            const int kt = az > 0 ? km : (az < 0 ? kp : kc);
+            const T x00 = lerp2(om, m, R(p, r00, A), R(p, r00, B));
             T y00 = x00;
-            if (ay != 0) {
-                const T x01 = lerp2(om, m, b0[sa + jo], b0[sa + jo + dxo]);
-                y00 = lerp2(P.ty_om, P.ty_m, x00, x01);
+            if (ay) {
+                const long long r10 = R.rb(jt, kc);
+                y00 = lerp2(P.ty_om, P.ty_m, x00, lerp2(om, m, R(p, r10, A), R(p, r10, B)));
             }
-            if (az != 0) {
-                const T x10 = lerp2(om, m, b1[sa], b1[sa + dxo]);
+            if (az) {
+                const long long r01 = R.rb(jc, kt);
+                const T x10 = lerp2(om, m, R(p, r01, A), R(p, r01, B));
                 T y11 = x10;
-                if (ay != 0) {
-                    const T x11 = lerp2(om, m, b1[sa + jo], b1[sa + jo + dxo]);
-                    y11 = lerp2(P.ty_om, P.ty_m, x10, x11);
+                if (ay) {
+                    const long long r11 = R.rb(jt, kt);
+                    y11 = lerp2(P.ty_om, P.ty_m, x10, lerp2(om, m, R(p, r11, A), R(p, r11, B)));
                 }
                 v[p] = lerp2(P.tz_om, P.tz_m, y00, y11);
             } else {
                 v[p] = y00;
             }
-        } else if (AX == 1) {
-            // x shift ii=-cx (transverse, per-column weight); y normal (anchor row, row above); z shift kk=-cz
-            const int io = -ax;
-            const T *b0 = base;
-            const T *b1 = az > 0 ? pM + p * PL : (az < 0 ? pP + p * PL : base);
+        }
+    } else if (AX == 1) {
+        // rows j (anchor) and j+1 (other); transverse x to column i - cx, z to plane k - cz
+        const long long rA = R.rb(jc, kc), rB = R.rb(jp, kc);
+        v[0] = T(0.5) * (R(0, rA, i) + R(0, rB, i));
+        const T *tw = P.txw + (size_t)i * 38;
+#pragma unroll
+        for (int p = 1; p < NPOP; ++p) {
+            const int ax = cx(p), az = cz(p);
+            const int io = i - ax;
+            const int kt = az > 0 ? km : (az < 0 ? kp : kc);
             T txo = T(1), txm = T(0);
-            if (ax != 0) {
-                txo = __ldg(P.txw + (size_t)gi * 38 + 2 * p);
-                txm = __ldg(P.txw + (size_t)gi * 38 + 2 * p + 1);
-            }
-            T x00 = b0[sa], x01 = b0[sa + PW];
-            if (ax != 0) {
-                x00 = lerp2(txo, txm, x00, b0[sa + io]);
-                x01 = lerp2(txo, txm, x01, b0[sa + PW + io]);
+            if (ax) { txo = __ldg(tw + 2 * p); txm = __ldg(tw + 2 * p + 1); }
+            T x00 = R(p, rA, i), x01 = R(p, rB, i);
+            if (ax) {
+                x00 = lerp2(txo, txm, x00, R(p, rA, io));
+                x01 = lerp2(txo, txm, x01, R(p, rB, io));
             }
             const T y00 = lerp2(P.yn_om[p], P.yn_m[p], x00, x01);
-            if (az != 0) {
-                T x10 = b1[sa], x11 = b1[sa + PW];
-                if (ax != 0) {
-                    x10 = lerp2(txo, txm, x10, b1[sa + io]);
-                    x11 = lerp2(txo, txm, x11, b1[sa + PW + io]);
+            if (az) {
+                const long long sA = R.rb(jc, kt), sB = R.rb(jp, kt);
+                T x10 = R(p, sA, i), x11 = R(p, sB, i);
+                if (ax) {
+                    x10 = lerp2(txo, txm, x10, R(p, sA, io));
+                    x11 = lerp2(txo, txm, x11, R(p, sB, io));
                 }
-                const T y11 = lerp2(P.yn_om[p], P.yn_m[p], x10, x11);
-                v[p] = lerp2(P.tz_om, P.tz_m, y00, y11);
+                v[p] = lerp2(P.tz_om, P.tz_m, y00, lerp2(P.yn_om[p], P.yn_m[p], x10, x11));
             } else {
                 v[p] = y00;
             }
-        } else {
-            // x shift ii=-cx, y shift jj=-cy, z normal (plane k anchor, plane k+1 other)
-            const int io = -ax, jo = -ay * PW;
-            const T *b0 = base, *b1 = pB + p * PL;
+        }
+    } else {
+        // planes k (anchor) and k+1 (other); transverse x to i - cx, y to row j - cy
+        const long long rA = R.rb(jc, kc), rB = R.rb(jc, kp);
+        v[0] = T(0.5) * (R(0, rA, i) + R(0, rB, i));
+        const T *tw = P.txw + (size_t)i * 38;
+#pragma unroll
+        for (int p = 1; p < NPOP; ++p) {
+            const int ax = cx(p), ay = cy(p);
+            const int io = i - ax;
+            const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
             T txo = T(1), txm = T(0);
-            if (ax != 0) {
-                txo = __ldg(P.txw + (size_t)gi * 38 + 2 * p);
-                txm = __ldg(P.txw + (size_t)gi * 38 + 2 * p + 1);
-            }
-            T x00 = b0[sa], x10 = b1[sa];
-            if (ax != 0) {
-                x00 = lerp2(txo, txm, x00, b0[sa + io]);
-                x10 = lerp2(txo, txm, x10, b1[sa + io]);
+            if (ax) { txo = __ldg(tw + 2 * p); txm = __ldg(tw + 2 * p + 1); }
+            T x00 = R(p, rA, i), x10 = R(p, rB, i);
+            if (ax) {
+                x00 = lerp2(txo, txm, x00, R(p, rA, io));
+                x10 = lerp2(txo, txm, x10, R(p, rB, io));
             }
             T y00 = x00, y11 = x10;
-            if (ay != 0) {
-                T x01 = b0[sa + jo], x11 = b1[sa + jo];
-                if (ax != 0) {
-                    x01 = lerp2(txo, txm, x01, b0[sa + jo + io]);
-                    x11 = lerp2(txo, txm, x11, b1[sa + jo + io]);
+            if (ay) {
+                const long long sA = R.rb(jt, kc), sB = R.rb(jt, kp);
+                T x01 = R(p, sA, i), x11 = R(p, sB, i);
+                if (ax) {
+                    x01 = lerp2(txo, txm, x01, R(p, sA, io));
+                    x11 = lerp2(txo, txm, x11, R(p, sB, io));
                 }
                 y00 = lerp2(P.ty_om, P.ty_m, x00, x01);
                 y11 = lerp2(P.ty_om, P.ty_m, x10, x11);
@@ -310,11 +363,61 @@ __device__ __forceinline__ void face_values(const StepParams<T, S> &P, const T *
     }
 }
 
+// 19 face values of the central-difference ("gradient") reconstruction,
+// f_face = mean - hdt (c . grad), src/dugks.cu:459-583 (calc_fx): normal
+// gradient across the face, transverse gradients of face-averaged neighbours
+// over two cells.  Uniform mesh.
+template <class T, class S, int AX>
+__device__ __forceinline__ void face_grad(const StepParams<T, S> &P, const FbRead<T, S> &R, int i, int j, int k,
+                                          T v[NPOP])
+{
+    const int ny = P.ny, nz = P.nz;
+    const int jm = wrap1(j - 1, ny), jp = wrap1(j + 1, ny), jc = wrap1(j, ny);
+    const int km = wrap1(k - 1, nz), kp = wrap1(k + 1, nz), kc = wrap1(k, nz);
+    const T h = P.hdt;
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) {
+        T temp, gx, gy, gz;
+        if (AX == 0) {
+            const int L = i, Rr = i + 1;  // left / right column of face I = i
+            const long long r = R.rb(jc, kc);
+            const T a = R(p, r, Rr), b = R(p, r, L);
+            temp = T(0.5) * (a + b);
+            gx = (a - b) * P.g_idx;
+            const long long ru = R.rb(jp, kc), rd = R.rb(jm, kc);
+            gy = (T(0.5) * (R(p, ru, L) + R(p, ru, Rr)) - T(0.5) * (R(p, rd, L) + R(p, rd, Rr))) * P.g_i2dy;
+            const long long rt = R.rb(jc, kp), rbo = R.rb(jc, km);
+            gz = (T(0.5) * (R(p, rt, L) + R(p, rt, Rr)) - T(0.5) * (R(p, rbo, L) + R(p, rbo, Rr))) * P.g_i2dz;
+        } else if (AX == 1) {
+            const long long rD = R.rb(jc, kc), rU = R.rb(jp, kc);
+            const T a = R(p, rU, i), b = R(p, rD, i);
+            temp = T(0.5) * (a + b);
+            gx = (T(0.5) * (R(p, rD, i + 1) + R(p, rU, i + 1)) - T(0.5) * (R(p, rD, i - 1) + R(p, rU, i - 1))) * P.g_i2dx;
+            gy = (a - b) * P.g_idy;
+            const long long tD = R.rb(jc, kp), tU = R.rb(jp, kp), bD = R.rb(jc, km), bU = R.rb(jp, km);
+            gz = (T(0.5) * (R(p, tD, i) + R(p, tU, i)) - T(0.5) * (R(p, bD, i) + R(p, bU, i))) * P.g_i2dz;
+        } else {
+            const long long rB = R.rb(jc, kc), rT = R.rb(jc, kp);
+            const T a = R(p, rT, i), b = R(p, rB, i);
+            temp = T(0.5) * (a + b);
+            gx = (T(0.5) * (R(p, rB, i + 1) + R(p, rT, i + 1)) - T(0.5) * (R(p, rB, i - 1) + R(p, rT, i - 1))) * P.g_i2dx;
+            const long long uB = R.rb(jp, kc), uT = R.rb(jp, kp), dB = R.rb(jm, kc), dT = R.rb(jm, kp);
+            gy = (T(0.5) * (R(p, uB, i) + R(p, uT, i)) - T(0.5) * (R(p, dB, i) + R(p, dT, i))) * P.g_i2dy;
+            gz = (a - b) * P.g_idz;
+        }
+        T s = T(0);
+        if (cx(p)) s += cx(p) > 0 ? gx : -gx;
+        if (cy(p)) s += cy(p) > 0 ? gy : -gy;
+        if (cz(p)) s += cz(p) > 0 ? gz : -gz;
+        v[p] = p == 0 ? temp : temp - h * s;
+    }
+}
+
 // Face equilibrium and flux (src/dugks.cu:675-709 f2ruvwh, 912-943):
 //   F_p = fw1 v_p + (fw2 + fw0 F.(c_p - u)/RT) feq_p(rho, u + hdt/2 F)
-// for the 10 populations crossing a face normal to AX, written to out[s*stride].
+// for the 10 populations crossing a face normal to AX, written to out[s].
 template <class T, class S, int AX>
-__device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[NPOP], T *out, int stride)
+__device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[NPOP], T out[10])
 {
     T r, jx, jy, jz;
     moments(v, r, jx, jy, jz);
@@ -353,7 +456,7 @@ __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[N
 #pragma unroll
     for (int s = 0; s < 10; ++s) {
         const int p = flux_pop(AX, s);
-        out[s * stride] = fma(B + P.Kf[p], fe[p], P.fw1 * v[p]);
+        out[s] = fma(B + P.Kf[p], fe[p], P.fw1 * v[p]);
     }
 }
 
@@ -370,167 +473,102 @@ __device__ __forceinline__ void bounce_back(T v[NPOP], bool lo, bool hi)
     }
 }
 
-template <class T, class S, int BX, int BY, int NT>
-__global__ void __launch_bounds__(NT) flux_kernel(const S *__restrict__ fb, const S *f_in, S *f_out,
-                                                   const StepParams<T, S> P, int kchunk)
+// Fluxes of one face: reconstruction + bounce-back + face equilibrium.
+template <class T, class S, int AX, int RECON>
+__device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const FbRead<T, S> &R, int i, int j, int k,
+                                            T out[10])
 {
-    using Tile = FluxTile<T, BX, BY>;
-    constexpr int PW = Tile::PW, PL = Tile::PL;
-    constexpr int NXF = Tile::NXF, NYF = Tile::NYF, NZF = Tile::NZF;
-    constexpr int NXFP = Tile::NXFP, NYFP = Tile::NYFP, NZFP = Tile::NZFP;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *planes = reinterpret_cast<T *>(smem_raw);     // [3][19][PL]
-    T *fxs = planes + 3 * NPOP * PL;                  // [10][NXF]
-    T *fys = fxs + 10 * NXF;                          // [10][NYF]
-    T *fzs = fys + 10 * NYF;                          // [2][10][NZF]
+    T v[NPOP];
+    if (RECON == 0)
+        face_tri<T, S, AX>(P, R, i, j, k, v);
+    else
+        face_grad<T, S, AX>(P, R, i, j, k, v);
+    if (AX == 0 && !P.periodic_x) bounce_back(v, i == 0, i == P.nx);
+    face_flux<T, S, AX>(P, v, out);
+}
 
+template <class T, class S, int W, int RECON>
+__global__ void __launch_bounds__(32 * W, 1) flux_kernel(const S *__restrict__ fb, const S *f_in, S *f_out,
+                                                       const StepParams<T, S> P, int kchunk)
+{
+    __shared__ T ysh[2][W][10][32];  // +y face fluxes of every warp row (double buffer)
+    __shared__ T xsh[2][W][10];      // -x face fluxes of the first column, one per row
+    const int lane = threadIdx.x, wr = threadIdx.y;
     const int nx = P.nx, ny = P.ny, nz = P.nz;
-    const int i0 = blockIdx.x * BX + 1;  // 1-based first cell of the tile
-    const int j0 = blockIdx.y * BY + 1;
+    const int i0 = blockIdx.x * 32 + 1;           // first column of the tile (1-based)
+    const int j0 = blockIdx.y * (W - 1) + 1;      // first row of the tile (1-based)
     const int kb = blockIdx.z * kchunk + 1;
-    const int ke = min(kb + kchunk, nz + 1);  // exclusive
-    const int tid = threadIdx.x;
-    const long long ps = P.ps;
+    const int ke = min(kb + kchunk, nz + 1);
+    const FbRead<T, S> R{fb, P.ps_b, P.pitch_b, ny, nz, P.codec};
 
-    // ---- stage plane g (1-based, 0..nz+1) of f-bar-plus into its buffer ----
-    auto load_plane = [&](int g) {
-        const int gz = g == 0 ? nz : (g == nz + 1 ? 1 : g);
-        T *dst = planes + (g % 3) * NPOP * PL;
-        const long long zoff = (long long)(gz - 1) * ny * P.pitch;
-        for (int e = tid; e < PL; e += NT) {
-            const int sj = e / PW, si = e - sj * PW;
-            int gi = i0 - 1 + si, gj = j0 - 1 + sj;
-            gj = gj == 0 ? ny : (gj == ny + 1 ? 1 : (gj > ny + 1 ? ny : gj));
-            int mode = 0;  // 0 plain, 1 left wall ghost, 2 right wall ghost
-            if (gi == 0) {
-                if (P.periodic_x) gi = nx; else mode = 1;
-            } else if (gi == nx + 1) {
-                if (P.periodic_x) gi = 1; else mode = 2;
-            } else if (gi > nx + 1) {
-                gi = nx;
-            }
-            const long long row = zoff + (long long)(gj - 1) * P.pitch;
-            if (mode == 0) {
-                const long long o = row + (gi - 1);
+    // warps 1..W-1: cell (gi, gj); warp 0: halo
+    const int gi = i0 + lane;
+    const int gj = j0 + wr - 1;
+    const bool cell = wr >= 1 && gi <= nx && gj <= ny;
+    const int ci = min(gi, nx);                     // clamped column for unused lanes
+    const int cj = wr >= 1 ? min(gj, ny) : 1;
+    // warp 0 tasks: y face J = j0-1 at column gi; -x face of row j0+lane (lanes < W-1)
+    const int hj = j0 + lane;                       // halo x-face row
+    const bool hx = wr == 0 && lane < W - 1 && hj <= ny;
+
+    T fzd[10], fzu[10], fx[10], fy[10];
+    int buf = 0;
+    if (kb >= ke) return;
+    if (wr >= 1) face_fluxes<T, S, 2, RECON>(P, R, ci, cj, kb - 1, fzd);  // z face kb-1/2
+    for (int k = kb; k < ke; ++k) {
+        if (wr >= 1) {
+            face_fluxes<T, S, 0, RECON>(P, R, ci, cj, k, fx);   // +x face I = gi
+            face_fluxes<T, S, 1, RECON>(P, R, ci, cj, k, fy);   // +y face J = gj
+            face_fluxes<T, S, 2, RECON>(P, R, ci, cj, k, fzu);  // +z face k+1/2
 #pragma unroll
-                for (int p = 0; p < NPOP; ++p) dst[p * PL + e] = P.codec.load_nc(fb, p * ps + o, p);
-            } else {
-                // linear extrapolation to the ghost cell centre (src/dugks.cu:1247-1248;
-                // stretched: src/fortran/channel/src/dugks.cuf:368-373)
-                const long long o1 = row + (mode == 1 ? 0 : nx - 1);
-                const long long o2 = row + (mode == 1 ? 1 : nx - 2);
-                const T q = mode == 1 ? P.q0 : P.q1;
+            for (int s = 0; s < 10; ++s) ysh[buf][wr][s][lane] = fy[s];
+        } else {
+            face_fluxes<T, S, 1, RECON>(P, R, ci, j0 - 1, k, fy);  // y face J = j0-1 (may be 0: periodic image)
+#pragma unroll
+            for (int s = 0; s < 10; ++s) ysh[buf][0][s][lane] = fy[s];
+            if (hx) {
+                T hxf[10];
+                face_fluxes<T, S, 0, RECON>(P, R, i0 - 1, hj, k, hxf);  // x face I = i0-1 of row hj
+#pragma unroll
+                for (int s = 0; s < 10; ++s) xsh[buf][lane + 1][s] = hxf[s];
+            }
+        }
+        __syncthreads();
+        if (wr >= 1) {
+            T fxl[10];
+#pragma unroll
+            for (int s = 0; s < 10; ++s) {
+                const T up = __shfl_up_sync(0xffffffffu, fx[s], 1);
+                fxl[s] = lane == 0 ? xsh[buf][wr][s] : up;
+            }
+            if (cell) {
+                const long long c = ((long long)(k - 1) * ny + (gj - 1)) * P.pitch + (gi - 1);
+                const long long cb = R.rb(gj, k) + gi;
+                const T cxg = __ldg(P.cxu + gi);
+                const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
 #pragma unroll
                 for (int p = 0; p < NPOP; ++p) {
-                    const T a = P.codec.load_nc(fb, p * ps + o1, p);
-                    const T b = P.codec.load_nc(fb, p * ps + o2, p);
-                    dst[p * PL + e] = q * a + (T(1) - q) * b;
+                    const T fo = P.codec.load(f_in, p * P.ps + c, p);
+                    T r = fma(R(p, cb, 0), c43, -(fo * c13));
+                    if (cx(p)) {
+                        const int s = flux_slot(0, p);
+                        r = fma(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s], r);
+                    }
+                    if (cy(p)) {
+                        const int s = flux_slot(1, p);
+                        r = fma(cy(p) > 0 ? -P.cyu : P.cyu, fy[s] - ysh[buf][wr - 1][s][lane], r);
+                    }
+                    if (cz(p)) {
+                        const int s = flux_slot(2, p);
+                        r = fma(cz(p) > 0 ? -P.czu : P.czu, fzu[s] - fzd[s], r);
+                    }
+                    P.codec.store(f_out, p * P.ps + c, p, r);
                 }
             }
-        }
-    };
-    auto plane = [&](int g) -> const T * { return planes + (g % 3) * NPOP * PL; };
-
-    // ---- reconstruct + flux of the faces of plane k (x, y and z=k+1/2) ----
-    auto faces = [&](int k, int zbuf, bool xy) {
-        const T *pk = plane(k), *pm = plane(k - 1), *pp = plane(k + 1);
-        const int njobs = xy ? NXFP + NYFP + NZFP : NZFP;
-        for (int q0 = tid; q0 < njobs; q0 += NT) {
-            int q = xy ? q0 : q0 + NXFP + NYFP;
-            T v[NPOP];
-            if (q < NXFP) {
-                if (q >= NXF) continue;
-                const int sj = q / (BX + 1), fi = q - sj * (BX + 1);
-                const int I = i0 - 1 + fi, gj = j0 + sj;
-                if (I > nx || gj > ny) continue;
-                const int sa = (sj + 1) * PW + (I == 0 ? fi + 1 : fi);
-                const int dxo = I == 0 ? -1 : 1;
-                face_values<T, S, 0, BX, BY>(P, pk, nullptr, pm, pp, sa, dxo, 0, P.xw + (size_t)I * 38, v);
-                if (!P.periodic_x) bounce_back(v, I == 0, I == nx);
-                face_flux<T, S, 0>(P, v, fxs + q, NXF);
-            } else if (q < NXFP + NYFP) {
-                q -= NXFP;
-                if (q >= NYF) continue;
-                const int fj = q / BX, si = q - fj * BX;
-                const int gi = i0 + si, J = j0 - 1 + fj;
-                if (gi > nx || J > ny) continue;
-                const int sa = fj * PW + si + 1;
-                face_values<T, S, 1, BX, BY>(P, pk, nullptr, pm, pp, sa, 0, gi, nullptr, v);
-                face_flux<T, S, 1>(P, v, fys + q, NYF);
-            } else {
-                q -= NXFP + NYFP;
-                if (q >= NZF) continue;
-                const int sj = q / BX, si = q - sj * BX;
-                const int gi = i0 + si, gj = j0 + sj;
-                if (gi > nx || gj > ny) continue;
-                const int sa = (sj + 1) * PW + si + 1;
-                face_values<T, S, 2, BX, BY>(P, pk, pp, nullptr, nullptr, sa, 0, gi, nullptr, v);
-                face_flux<T, S, 2>(P, v, fzs + zbuf * 10 * NZF + q, NZF);
-            }
-        }
-    };
-
-    // ---- finite-volume update of plane k (src/dugks.cu:945-956) ----
-    auto update = [&](int k, int zbot, int ztop) {
-        const T *pk = plane(k);
-        const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
-        for (int q = tid; q < BX * BY; q += NT) {
-            const int sj = q / BX, si = q - sj * BX;
-            const int gi = i0 + si, gj = j0 + sj;
-            if (gi > nx || gj > ny) continue;
-            const long long c = ((long long)(k - 1) * ny + (gj - 1)) * P.pitch + (gi - 1);
-            const T cxg = __ldg(P.cxu + gi);
-            const int sc = (sj + 1) * PW + si + 1;
 #pragma unroll
-            for (int p = 0; p < NPOP; ++p) {
-                const T fo = P.codec.load(f_in, p * ps + c, p);
-                T r = fma(pk[p * PL + sc], c43, -(fo * c13));
-                if (cx(p)) {
-                    const int s = flux_slot(0, p);
-                    const T d = fxs[s * NXF + sj * (BX + 1) + si + 1] - fxs[s * NXF + sj * (BX + 1) + si];
-                    r = fma(cx(p) > 0 ? -cxg : cxg, d, r);
-                }
-                if (cy(p)) {
-                    const int s = flux_slot(1, p);
-                    const T d = fys[s * NYF + (sj + 1) * BX + si] - fys[s * NYF + sj * BX + si];
-                    r = fma(cy(p) > 0 ? -P.cyu : P.cyu, d, r);
-                }
-                if (cz(p)) {
-                    const int s = flux_slot(2, p);
-                    const T d = fzs[ztop * 10 * NZF + s * NZF + q] - fzs[zbot * 10 * NZF + s * NZF + q];
-                    r = fma(cz(p) > 0 ? -P.czu : P.czu, d, r);
-                }
-                P.codec.store(f_out, p * ps + c, p, r);
-            }
+            for (int s = 0; s < 10; ++s) fzd[s] = fzu[s];
         }
-    };
-
-    if (kb >= ke) return;
-    load_plane(kb - 1);
-    load_plane(kb);
-    load_plane(kb + 1);
-    __syncthreads();
-    {
-        // bottom z face of the chunk (kb-1/2): anchor plane kb-1, other plane kb
-        const T *pa = plane(kb - 1), *pb = plane(kb);
-        for (int q = tid; q < NZF; q += NT) {
-            const int sj = q / BX, si = q - sj * BX;
-            const int gi = i0 + si, gj = j0 + sj;
-            if (gi > nx || gj > ny) continue;
-            T v[NPOP];
-            face_values<T, S, 2, BX, BY>(P, pa, pb, nullptr, nullptr, (sj + 1) * PW + si + 1, 0, gi, nullptr, v);
-            face_flux<T, S, 2>(P, v, fzs + q, NZF);
-        }
-    }
-    faces(kb, 1, true);
-    __syncthreads();
-    for (int k = kb; k < ke; ++k) {
-        const int zbot = (k - kb) & 1, ztop = zbot ^ 1;
-        if (k + 2 <= ke) load_plane(k + 2);
-        update(k, zbot, ztop);
-        __syncthreads();
-        if (k + 1 < ke) faces(k + 1, zbot, true);
-        __syncthreads();
+        buf ^= 1;
     }
 }
 

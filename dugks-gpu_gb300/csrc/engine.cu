@@ -115,6 +115,8 @@ struct dg_ctx {
     // derived
     int pitch = 0;
     long long ps = 0;
+    int pitch_b = 0;        // f-bar-plus: x ghost columns stored
+    long long ps_b = 0;
     std::vector<double> xf, xc, dxx;  // stretched mesh, xc/dxx indexed 0..nx+1
     RefCoef<double> c64{};
     RefCoef<float> c32{};
@@ -128,6 +130,9 @@ struct dg_ctx {
     double *macro = nullptr;      // rho|ux|uy|uz ghosted
     double *scratch = nullptr;    // statistics partial sums / moments partials
     size_t scratch_bytes = 0;
+    void *adj = nullptr;          // per-face adjoint scratch (allocated on first dg_adjoint_step)
+    double *acc = nullptr;        // running sums of the per-x statistics (dg_stats_accumulate)
+    long long acc_count = 0;
     bool macro_valid = false;
 
     ~dg_ctx()
@@ -137,6 +142,8 @@ struct dg_ctx {
         if (tab) cudaFree(tab);
         if (macro) cudaFree(macro);
         if (scratch) cudaFree(scratch);
+        if (adj) cudaFree(adj);
+        if (acc) cudaFree(acc);
     }
     int fail(int code, const std::string &msg)
     {
@@ -210,7 +217,6 @@ int load_config(dg_ctx *h, const ConfigFile &cf)
         return h->fail(DG_ERR_CONFIG, "CFL and the widths must be > 0");
     if (h->mesh != 0 && h->periodic[0]) return h->fail(DG_ERR_CONFIG, "a stretched mesh needs walls in x (periods_x=0)");
     if (h->recon == 1 && h->mesh != 0) return h->fail(DG_ERR_UNSUPPORTED, "recon=gradient needs a uniform mesh");
-    if (h->recon == 1) return h->fail(DG_ERR_UNSUPPORTED, "recon=gradient is not built in this engine yet");
     return DG_OK;
 }
 
@@ -331,6 +337,7 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     StepParams<T, S> P;
     std::memset(&P, 0, sizeof(P));
     P.nx = h->nx; P.ny = h->ny; P.nz = h->nz; P.pitch = h->pitch; P.ps = h->ps;
+    P.pitch_b = h->pitch_b; P.ps_b = h->ps_b;
     P.periodic_x = h->periodic[0];
     P.perturb = h->perturb;
     P.force_on = (c.F[0] != 0 || c.F[1] != 0 || c.F[2] != 0) ? 1 : 0;
@@ -354,6 +361,8 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     P.tz_m = T(tz); P.tz_om = T(R(1 - tz));
     P.cyu = T(c.dt / c.dy);
     P.czu = T(c.dt / c.dz);
+    P.g_idx = T(R(1) / c.dx); P.g_idy = T(R(1) / c.dy); P.g_idz = T(R(1) / c.dz);
+    P.g_i2dx = T(R(1) / (2 * c.dx)); P.g_i2dy = T(R(1) / (2 * c.dy)); P.g_i2dz = T(R(1) / (2 * c.dz));
     if (h->mesh != 0) {
         const int nx = h->nx;
         P.q0 = T((h->xc[2] - h->xc[0]) / (h->xc[2] - h->xc[1]));                  // dugks.cuf:368
@@ -433,7 +442,7 @@ int step_form(dg_ctx *h, int istep0, int n, cudaEvent_t *ev)
         if (h->perturb && s > 0) P = params_for<T, S>(h, istep0 + s);
         CK(K::fbar(f, fb, P, h->stream), "stage (a) launch");
         if (ev) CK(cudaEventRecord(ev[2 * s + 1], h->stream), "event record");
-        CK(K::flux(fb, f, f, P, h->stream), "flux launch");
+        CK(K::flux(fb, f, f, P, h->recon, h->stream), "flux launch");
         if (ev) CK(cudaEventRecord(ev[2 * s + 2], h->stream), "event record");
     }
     h->macro_valid = false;
@@ -524,6 +533,30 @@ int stats_form(dg_ctx *h, std::vector<double> &total)
     return DG_OK;
 }
 
+// one statistics pass into the device running sums (no host transfer)
+template <class T, class S>
+int accumulate_form(dg_ctx *h)
+{
+    using K = Kern<T, S>;
+    const int nb = stats_blocks(h);
+    const size_t part = size_t(nb) * h->nx * NSTAT;
+    int rc = ensure_scratch(h, (part + size_t(h->nx) * NSTAT) * sizeof(double));
+    if (rc) return rc;
+    if (!h->acc) {
+        CK(cudaMalloc(&h->acc, size_t(h->nx) * 10 * sizeof(double)), "cudaMalloc (statistics accumulator)");
+        CK(cudaMemsetAsync(h->acc, 0, size_t(h->nx) * 10 * sizeof(double), h->stream), "cudaMemset (accumulator)");
+        h->acc_count = 0;
+    }
+    double *partial = h->scratch, *tot = h->scratch + part;
+    CK(K::stats_partials(static_cast<const S *>(h->f), params_for<T, S>(h, 0), h->hdt(), h->F, partial, nb, h->stream),
+       "statistics launch");
+    CK(launch_stats_reduce(partial, nb, h->nx, tot, h->stream), "statistics reduce launch");
+    stats_accumulate_kernel<<<(h->nx * 10 + 127) / 128, 128, 0, h->stream>>>(tot, h->nx, h->acc);
+    CK(cudaGetLastError(), "accumulate launch");
+    h->acc_count++;
+    return DG_OK;
+}
+
 template <class T, class S>
 int moments_form(dg_ctx *h, double *out4)
 {
@@ -540,6 +573,22 @@ int moments_form(dg_ctx *h, double *out4)
     for (int m = 0; m < 4; ++m) out4[m] = 0;
     for (int b = 0; b < nb; ++b)
         for (int m = 0; m < 4; ++m) out4[m] += part[size_t(b) * 4 + m];
+    return DG_OK;
+}
+
+template <class T, class S>
+int adjoint_form(dg_ctx *h, int istep, const void *f_n, const void *lam_next, void *lam_out)
+{
+    using K = Kern<T, S>;
+    if (!std::is_same<T, S>::value) return h->fail(DG_ERR_UNSUPPORTED, "the adjoint exists for the fp64 and fp32 forms");
+    if (!h->adj) {
+        const long long n = adj_nface(0, h->nx, h->ny, h->nz) + 2 * adj_nface(1, h->nx, h->ny, h->nz);
+        CK(cudaMalloc(&h->adj, size_t(n) * NPOP * sizeof(T)), "cudaMalloc (adjoint scratch)");
+    }
+    CK(K::adjoint(static_cast<const S *>(f_n), static_cast<S *>(h->fb), static_cast<const S *>(lam_next),
+                  static_cast<S *>(lam_out), static_cast<T *>(h->adj), params_for<T, S>(h, istep), h->stream),
+       "adjoint launch");
+    h->macro_valid = false;
     return DG_OK;
 }
 
@@ -582,11 +631,14 @@ int allocate(dg_ctx *h)
     const long long plane = (long long)h->pitch * h->ny * h->nz;
     const long long a256 = 256 / (long long)sb;
     h->ps = (plane + a256 - 1) / a256 * a256;
-    const size_t bytes = size_t(h->ps) * 19 * sb;
+    h->pitch_b = (h->nx + 2 + align - 1) / align * align;
+    const long long plane_b = (long long)h->pitch_b * h->ny * h->nz;
+    h->ps_b = (plane_b + a256 - 1) / a256 * a256;
+    const size_t bytes = size_t(h->ps) * 19 * sb, bytes_b = size_t(h->ps_b) * 19 * sb;
     CK(cudaMalloc(&h->f, bytes), "cudaMalloc (f)");
-    CK(cudaMalloc(&h->fb, bytes), "cudaMalloc (fb)");
+    CK(cudaMalloc(&h->fb, bytes_b), "cudaMalloc (fb)");
     CK(cudaMemset(h->f, 0, bytes), "cudaMemset (f)");
-    CK(cudaMemset(h->fb, 0, bytes), "cudaMemset (fb)");
+    CK(cudaMemset(h->fb, 0, bytes_b), "cudaMemset (fb)");
     return h->prec == DG_PREC_FP64 ? upload_tables<double>(h) : upload_tables<float>(h);
 }
 
@@ -782,6 +834,15 @@ cudaError_t launch_stats_reduce(const double *partial, int nblocks, int nx, doub
 {
     stats_reduce_kernel<<<(nx + 127) / 128, 128, 0, st>>>(partial, nblocks, nx, total);
     return cudaGetLastError();
+}
+
+// acc[i][s] += total[i][s] for the 10 sums (rho, u, v, w, uw, uv, vw, uu, vv, ww)
+__global__ void stats_accumulate_kernel(const double *__restrict__ total, int nx, double *__restrict__ acc)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nx * 10) return;
+    const int i = q / 10, s = q % 10;
+    acc[q] += total[size_t(i) * NSTAT + s];
 }
 }  // namespace dg
 
@@ -1141,6 +1202,73 @@ const void *dg_device_ptr(const dg_t *h, int which)
     case DG_BUF_UZ: return h->macro ? h->macro + 3 * g : nullptr;
     }
     return nullptr;
+}
+
+int dg_adjoint_step(dg_t *h, int istep, const void *f_n, const void *lam_next, void *lam_out)
+{
+    if (!h || !f_n || !lam_next || !lam_out) return DG_ERR_ARG;
+    if (f_n == h->fb || lam_next == h->fb || lam_out == h->fb || f_n == lam_out)
+        return h->fail(DG_ERR_ARG, "adjoint buffers must not alias f-bar-plus or each other (lam_out may equal lam_next)");
+    return DISPATCH(h, adjoint_form, istep, f_n, lam_next, lam_out);
+}
+
+int dg_get_state_device(dg_t *h, void *dst)
+{
+    if (!h || !dst) return DG_ERR_ARG;
+    CK(cudaMemcpyAsync(dst, h->f, size_t(h->ps) * 19 * storage_bytes(h->prec), cudaMemcpyDeviceToDevice, h->stream),
+       "state copy (device)");
+    return DG_OK;
+}
+
+int dg_set_state_device(dg_t *h, const void *src)
+{
+    if (!h || !src) return DG_ERR_ARG;
+    CK(cudaMemcpyAsync(h->f, src, size_t(h->ps) * 19 * storage_bytes(h->prec), cudaMemcpyDeviceToDevice, h->stream),
+       "state copy (device)");
+    h->macro_valid = false;
+    return DG_OK;
+}
+
+int dg_stats_accumulate(dg_t *h)
+{
+    if (!h) return DG_ERR_ARG;
+    return DISPATCH(h, accumulate_form);
+}
+
+int dg_stats_accumulated(dg_t *h, double *prof9, long long *count)
+{
+    if (!h) return DG_ERR_ARG;
+    if (count) *count = h->acc_count;
+    if (!prof9) return DG_OK;
+    const int nx = h->nx;
+    std::vector<double> a(size_t(nx) * 10, 0.0);
+    if (h->acc) {
+        CK(cudaMemcpyAsync(a.data(), h->acc, a.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+           "accumulator copy");
+        CK(cudaStreamSynchronize(h->stream), "accumulator sync");
+    }
+    const double n = double(h->ny) * h->nz * double(h->acc_count > 0 ? h->acc_count : 1);
+    for (int i = 0; i < nx; ++i) {
+        const double *t = &a[size_t(i) * 10];
+        const double ua = t[1] / n, va = t[2] / n, wa = t[3] / n;
+        double *o = prof9 + 9 * size_t(i);
+        o[0] = ua; o[1] = va; o[2] = wa;
+        o[3] = t[4] / n - ua * wa;
+        o[4] = t[5] / n - ua * va;
+        o[5] = t[6] / n - va * wa;
+        o[6] = t[7] / n - ua * ua;
+        o[7] = t[8] / n - va * va;
+        o[8] = t[9] / n - wa * wa;
+    }
+    return DG_OK;
+}
+
+int dg_stats_reset(dg_t *h)
+{
+    if (!h) return DG_ERR_ARG;
+    if (h->acc) CK(cudaMemsetAsync(h->acc, 0, size_t(h->nx) * 10 * sizeof(double), h->stream), "cudaMemset (accumulator)");
+    h->acc_count = 0;
+    return DG_OK;
 }
 
 int dg_get_mesh(const dg_t *h, double *xc, double *dxx)

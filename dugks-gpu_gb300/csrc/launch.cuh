@@ -5,24 +5,28 @@
 #include <cuda_runtime.h>
 #include "dugks_kernels.cuh"
 #include "aux_kernels.cuh"
+#include "adjoint_kernels.cuh"
 
 namespace dg {
 
-// Flux-kernel tile per form: BX x BY cells, NT threads.
+// Flux-kernel CTA per form: W warps = W-1 rows of 32 cells plus the halo warp.
 template <class T, class S>
 struct TileCfg {
-    static constexpr int BX = 32, BY = 4, NT = 128;
+    static constexpr int W = 9;   // 8 rows of 32 cells; ~145 registers in FP32
 };
 template <>
 struct TileCfg<double, double> {
-    static constexpr int BX = 32, BY = 4, NT = 128;
+    static constexpr int W = 8;   // 7 rows; the FP64 kernel takes 255 registers at 256 threads
 };
 
 template <class T, class S>
 struct Kern {
+    // stage (a) and the x ghost columns of f-bar-plus
     static cudaError_t fbar(const S *f, S *fb, const StepParams<T, S> &P, cudaStream_t st);
+    // stages (b)-(e); recon 0 trilinear, 1 central-difference gradient.
     // f_in may equal f_out (in-place update, as the reference)
-    static cudaError_t flux(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P, cudaStream_t st);
+    static cudaError_t flux(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P, int recon,
+                            cudaStream_t st);
     static cudaError_t macro(const S *f, const StepParams<T, S> &P, double hdt, const double F[3], double *rho,
                              double *ux, double *uy, double *uz, cudaStream_t st);
     static cudaError_t aos_to_soa(const double *src, S *dst, const StepParams<T, S> &P, cudaStream_t st);
@@ -31,7 +35,11 @@ struct Kern {
                                       double *partial, int nblocks, cudaStream_t st);
     static cudaError_t moments_partials(const S *f, const StepParams<T, S> &P, double *partial, int nblocks,
                                         cudaStream_t st);
-    static size_t flux_smem_bytes();
+    // Adjoint of one step (adjoint_kernels.cuh): recomputes f-bar-plus of f_n into fb,
+    // per-face adjoints into lamv (T-typed scratch, adj_nface(0)+2*adj_nface(1) faces x 19),
+    // then lam_out = (dS/df)^T lam_next.  FP64 and FP32 forms only.
+    static cudaError_t adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_out, T *lamv,
+                               const StepParams<T, S> &P, cudaStream_t st);
     static int flux_kchunk(const StepParams<T, S> &P);
 };
 

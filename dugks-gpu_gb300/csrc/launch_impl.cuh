@@ -1,6 +1,7 @@
 // Template bodies of the launchers declared in launch.cuh.
 #pragma once
 #include <algorithm>
+#include <type_traits>
 #include "launch.cuh"
 
 namespace dg {
@@ -11,51 +12,42 @@ cudaError_t Kern<T, S>::fbar(const S *f, S *fb, const StepParams<T, S> &P, cudaS
     const int bx = P.nx >= 128 ? 128 : ((P.nx + 31) / 32) * 32;
     dim3 grid((P.nx + bx - 1) / bx, P.ny, P.nz);
     fbar_kernel<T, S><<<grid, bx, 0, st>>>(f, fb, P);
+    const long long rows = (long long)P.ny * P.nz;
+    fb_ghost_kernel<T, S><<<unsigned((rows + 255) / 256), 256, 0, st>>>(fb, P);
     return cudaGetLastError();
-}
-
-template <class T, class S>
-size_t Kern<T, S>::flux_smem_bytes()
-{
-    using C = TileCfg<T, S>;
-    return FluxTile<T, C::BX, C::BY>::bytes;
 }
 
 template <class T, class S>
 int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
 {
-    using C = TileCfg<T, S>;
+    constexpr int W = TileCfg<T, S>::W;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int occ = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, C::BX, C::BY, C::NT>, C::NT,
-                                                  flux_smem_bytes());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0>, 32 * W, 0);
     occ = std::max(occ, 1);
-    const long long cols = (long long)((P.nx + C::BX - 1) / C::BX) * ((P.ny + C::BY - 1) / C::BY);
+    const long long cols = (long long)((P.nx + 31) / 32) * ((P.ny + W - 2) / (W - 1));
     const long long want = 4LL * sms * occ;
     long long nchunks = (want + cols - 1) / cols;
     nchunks = std::max(1LL, std::min<long long>(nchunks, P.nz));
-    // at least 4 planes per chunk keeps the halo-plane overhead below 50 %
-    nchunks = std::min<long long>(nchunks, std::max(1, P.nz / 4));
+    // at least 8 planes per chunk keeps the extra bottom-face evaluation below 1/8
+    nchunks = std::min<long long>(nchunks, std::max(1, P.nz / 8));
     return int((P.nz + nchunks - 1) / nchunks);
 }
 
 template <class T, class S>
-cudaError_t Kern<T, S>::flux(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P, cudaStream_t st)
+cudaError_t Kern<T, S>::flux(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P, int recon,
+                             cudaStream_t st)
 {
-    using C = TileCfg<T, S>;
-    auto kern = flux_kernel<T, S, C::BX, C::BY, C::NT>;
-    const size_t smem = flux_smem_bytes();
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    constexpr int W = TileCfg<T, S>::W;
     const int kchunk = flux_kchunk(P);
-    dim3 grid((P.nx + C::BX - 1) / C::BX, (P.ny + C::BY - 1) / C::BY, (P.nz + kchunk - 1) / kchunk);
-    kern<<<grid, C::NT, smem, st>>>(fb, f_in, f_out, P, kchunk);
+    dim3 grid((P.nx + 31) / 32, (P.ny + W - 2) / (W - 1), (P.nz + kchunk - 1) / kchunk);
+    dim3 block(32, W);
+    if (recon == 1)
+        flux_kernel<T, S, W, 1><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
+    else
+        flux_kernel<T, S, W, 0><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
     return cudaGetLastError();
 }
 
@@ -103,6 +95,28 @@ cudaError_t Kern<T, S>::moments_partials(const S *f, const StepParams<T, S> &P, 
 {
     moments_partials_kernel<T, S><<<nblocks, 256, 0, st>>>(f, P, partial);
     return cudaGetLastError();
+}
+
+template <class T, class S>
+cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_out, T *lamv,
+                                const StepParams<T, S> &P, cudaStream_t st)
+{
+    if constexpr (!std::is_same<T, S>::value) {
+        return cudaErrorNotSupported;
+    } else {
+        cudaError_t e = fbar(f_n, fb, P, st);
+        if (e != cudaSuccess) return e;
+        const long long nfx = adj_nface(0, P.nx, P.ny, P.nz), nfc = adj_nface(1, P.nx, P.ny, P.nz);
+        T *LX = lamv, *LY = lamv + NPOP * nfx, *LZ = LY + NPOP * nfc;
+        adj_face_kernel<T, S, 0><<<unsigned((nfx + 127) / 128), 128, 0, st>>>(fb, lam_next, LX, P);
+        adj_face_kernel<T, S, 1><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LY, P);
+        adj_face_kernel<T, S, 2><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LZ, P);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        dim3 grid((P.nx + 127) / 128, P.ny, P.nz);
+        adj_gather_kernel<T, S><<<grid, 128, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, P);
+        return cudaGetLastError();
+    }
 }
 
 }  // namespace dg

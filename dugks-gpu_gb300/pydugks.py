@@ -93,6 +93,12 @@ def lib():
         "dg_device_ptr": (ctypes.c_void_p, [H, ctypes.c_int]),
         "dg_moments": (ctypes.c_int, [H, _D]),
         "dg_get_mesh": (ctypes.c_int, [H, _D, _D]),
+        "dg_stats_accumulate": (ctypes.c_int, [H]),
+        "dg_stats_accumulated": (ctypes.c_int, [H, _D, ctypes.POINTER(ctypes.c_longlong)]),
+        "dg_stats_reset": (ctypes.c_int, [H]),
+        "dg_get_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
+        "dg_set_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
+        "dg_adjoint_step": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -271,6 +277,18 @@ class Engine:
     def output_2d(self, step):
         self._check(lib().dg_output_2d(self._h, step))
 
+    def stats_accumulate(self):
+        self._check(lib().dg_stats_accumulate(self._h))
+
+    def stats_accumulated(self):
+        prof = np.empty((self.nx, 9), dtype=np.float64)
+        n = ctypes.c_longlong(0)
+        self._check(lib().dg_stats_accumulated(self._h, _ptr(prof), ctypes.byref(n)))
+        return prof, n.value
+
+    def stats_reset(self):
+        self._check(lib().dg_stats_reset(self._h))
+
     def moments(self):
         m = np.empty(4, dtype=np.float64)
         self._check(lib().dg_moments(self._h, _ptr(m)))
@@ -281,6 +299,21 @@ class Engine:
         dxx = np.empty(self.nx + 2)
         self._check(lib().dg_get_mesh(self._h, _ptr(xc), _ptr(dxx)))
         return xc, dxx
+
+    # device-resident state in the engine's SoA layout (19 * pop_stride elements)
+    @property
+    def soa_len(self):
+        return 19 * self.info.pop_stride
+
+    def get_state_device(self, dst_ptr):
+        self._check(lib().dg_get_state_device(self._h, ctypes.c_void_p(dst_ptr)))
+
+    def set_state_device(self, src_ptr):
+        self._check(lib().dg_set_state_device(self._h, ctypes.c_void_p(src_ptr)))
+
+    def adjoint_step(self, istep, f_ptr, lam_next_ptr, lam_out_ptr):
+        self._check(lib().dg_adjoint_step(self._h, istep, ctypes.c_void_p(f_ptr), ctypes.c_void_p(lam_next_ptr),
+                                          ctypes.c_void_p(lam_out_ptr)))
 
     def device_ptr(self, which):
         return lib().dg_device_ptr(self._h, which)

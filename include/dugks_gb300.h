@@ -44,7 +44,7 @@ typedef struct dg_ctx dg_t;
 
 /* device buffers exposed read-only (dg_device_ptr) */
 #define DG_BUF_F 0              /* f-tilde, structure of arrays */
-#define DG_BUF_FB 1             /* f-bar-plus, structure of arrays */
+#define DG_BUF_FB 1             /* f-bar-plus, structure of arrays with x ghost columns 0, nx+1 */
 #define DG_BUF_RHO 2            /* ghosted scalar macro arrays (after dg_upload_macro) */
 #define DG_BUF_UX 3
 #define DG_BUF_UY 4
@@ -131,6 +131,16 @@ int dg_stats(dg_t *h, int step);
  * src/output.cu:152-218 (output_2d, src/output.cu:118-147). */
 int dg_output_2d(dg_t *h, int step);
 
+/* Time-averaged statistics (an extension; the reference writes instantaneous
+ * profiles only): dg_stats_accumulate adds the current per-x plane sums of
+ * u, v, w and their products into FP64 device accumulators;
+ * dg_stats_accumulated returns the averages over all accumulated samples in
+ * the profiles-2.dat layout (9 values per x index: means, covariances
+ * <uw>', <uv>', <vw>', variances) and the sample count; dg_stats_reset clears. */
+int dg_stats_accumulate(dg_t *h);
+int dg_stats_accumulated(dg_t *h, double *prof9, long long *count);
+int dg_stats_reset(dg_t *h);
+
 /* --- state and checkpoint I/O ------------------------------------------ */
 
 /* Full ghosted AoS copy of f-tilde (src/dugks.cu:407-416 copy_ddf); ghost
@@ -154,6 +164,18 @@ const void *dg_device_ptr(const dg_t *h, int which);
 
 /* Total mass, x/y/z momentum of the current state in FP64. */
 int dg_moments(dg_t *h, double *mass_mom4);
+
+/* Device-to-device copy of the state in the engine's own SoA layout
+ * (19 * pop_stride elements of the storage type, see dg_info_t), on the
+ * handle's stream. */
+int dg_get_state_device(dg_t *h, void *dst);
+int dg_set_state_device(dg_t *h, const void *src);
+
+/* Hand-written adjoint of step `istep` (no counterpart in the reference):
+ * lam_out = (dS/df)^T lam_next at the state f_n, all three device arrays in
+ * the engine's SoA layout (fp64 and fp32 forms).  Recomputes f-bar-plus of
+ * f_n; lam_out may equal lam_next.  Asynchronous on the handle's stream. */
+int dg_adjoint_step(dg_t *h, int istep, const void *f_n, const void *lam_next, void *lam_out);
 
 /* Cell centres and widths along x, nx+2 entries each (index 0 and nx+1 are
  * the mirrored ghosts of src/fortran/channel/src/dugks.cuf:118-121); either

@@ -38,6 +38,25 @@ def test_fp32_matches_oracle(case):
     assert err <= FP32_TOL
 
 
+@pytest.mark.parametrize("case", ["walls", "periodic", "aniso"])
+def test_gradient_reconstruction_matches_oracle(case):
+    """recon=gradient: the central-difference variant of src/dugks.cu:421-649 (calc_fx)."""
+    from _cases import CASES as C
+    import pydugks
+    import pyoracle
+    from seeded import seeded_state
+    kw = dict(C[case])
+    kw["recon"] = "gradient"
+    eng = pydugks.Engine(pydugks.make_config(**kw))
+    orc = pyoracle.Oracle.from_engine_info(eng.info, recon=1)
+    f0 = seeded_state(eng.nx, eng.ny, eng.nz, seed=3)
+    eng.set_state(f0)
+    got, want = run_both(eng, orc, f0, 1, 20)
+    err = rel_err(got, want)
+    print(f"{case} gradient fp64 20 steps: rel err {err:.3e}")
+    assert err <= FP64_TOL
+
+
 def test_step_is_deterministic():
     eng, _, f0 = make_pair("walls", "fp64")
     eng.run(1, 5)

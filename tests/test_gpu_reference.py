@@ -73,15 +73,18 @@ def test_engine_matches_reference_fp32(case):
     assert err <= 2e-5
 
 
-def test_gradient_option_reference_runs():
-    """calc_fx (the central-difference variant) runs through the same harness."""
+def test_gradient_option_matches_reference():
+    """calc_fx (the central-difference variant): oracle and engine against the reference kernel."""
     _need_ref()
     kw = dict(REF_CASES["walls"])
     f0 = seeded_state(kw["nx"], kw["ny"], kw["nz"], seed=5)
     ref = pyoracle.to_ghosted(f0)
     pyoracle.ref_run(ref, **_ref_args(kw), istep0=1, nsteps=5, prec=0, recon=1)
-    eng = pydugks.Engine(pydugks.make_config(**kw))
+    eng = pydugks.Engine(pydugks.make_config(recon="gradient", **kw))
     orc = pyoracle.Oracle.from_engine_info(eng.info, recon=1)
     g = pyoracle.to_ghosted(f0)
     orc.run(g, 1, 5)
     assert rel_err(pyoracle.interior(g), pyoracle.interior(ref)) <= 1e-13
+    eng.set_state(f0)
+    eng.run(1, 5)
+    assert rel_err(eng.get_state(), pyoracle.interior(ref)) <= 1e-12
