@@ -29,6 +29,9 @@ DG_ERR_UNSUPPORTED = -7
 
 PREC = {"fp64": 0, "fp32": 1, "fp16": 2, "bf16": 3}
 
+DG_BUF_F = 0   # f-tilde, SoA
+DG_BUF_FB = 1  # f-bar-plus, SoA with x ghost columns
+
 # Keys read by the reference (src/numerics.cu:70-99, src/parallel.cu:95-97,
 # src/cuda.cu:17), in the order of examples/laminar/config.txt.
 REFERENCE_KEYS = ("case", "xwidth", "ywidth", "zwidth", "nx", "ny", "nz", "restart", "nrestart", "perturb",
@@ -96,6 +99,11 @@ def lib():
         "dg_stats_accumulate": (ctypes.c_int, [H]),
         "dg_stats_accumulated": (ctypes.c_int, [H, _D, ctypes.POINTER(ctypes.c_longlong)]),
         "dg_stats_reset": (ctypes.c_int, [H]),
+        "dg_stats_values_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                    ctypes.c_int, ctypes.c_longlong, ctypes.c_double,
+                                                    ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                                    ctypes.c_void_p, ctypes.c_void_p]),
+        "dg_noalloc_last_error": (ctypes.c_char_p, []),
         "dg_get_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
         "dg_set_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
         "dg_adjoint_step": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),

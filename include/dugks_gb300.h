@@ -182,6 +182,36 @@ int dg_adjoint_step(dg_t *h, int istep, const void *f_n, const void *lam_next, v
  * pointer may be NULL. */
 int dg_get_mesh(const dg_t *h, double *xc, double *dxx);
 
+/* --- allocation-free statistics (no counterpart in the reference) ------ */
+
+/* Largest nx accepted by dg_stats_values_noalloc. */
+#define DG_NOALLOC_MAX_NX 512
+
+/* The statistics of dg_stats_values (diag.dat and profiles-2.dat values) for
+ * callers that cannot allocate device memory at the point where they need
+ * them: code running under CUDA stream capture, where cudaMalloc is not
+ * allowed, and host programs whose own allocator owns all device memory and
+ * forbids later cudaMalloc calls.  This entry point allocates nothing; its
+ * scratch is a fixed array in the library's device image (about 5 MB, present
+ * on every GPU that loads the library until the process exits).
+ *   f      FP64 state in device memory in the engine's SoA layout, e.g.
+ *          dg_device_ptr(h, DG_BUF_F) of an fp64 engine, with nx <=
+ *          DG_NOALLOC_MAX_NX and pitch / pop_stride as in dg_info_t
+ *   hdt, fx, fy, fz   the velocity shift hdt*F of the macro output
+ *   out    device array of 12 + 9*nx + 1 doubles: the 12 diag values, the
+ *          nx x 9 profile values, then the number of cells with a non-finite
+ *          moment
+ * Asynchronous on `stream` (a cudaStream_t; 0 = legacy default stream).
+ * The first call on a device looks up the scratch array's device address with
+ * that device current; make that first call before any stream capture.  All
+ * calls share the one scratch array and each overwrites it completely: calls
+ * whose kernels can overlap on the GPU race on it and must be ordered by the
+ * caller.  nx beyond the maximum returns DG_ERR_SHAPE; the message of the
+ * last failure is dg_noalloc_last_error(). */
+int dg_stats_values_noalloc(const double *f, int nx, int ny, int nz, int pitch, long long pop_stride,
+                            double hdt, double fx, double fy, double fz, double *out, void *stream);
+const char *dg_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
