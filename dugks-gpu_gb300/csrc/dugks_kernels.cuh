@@ -48,6 +48,8 @@ struct StepParams {
     T fw1, fw2, fw0x3;           // fw0x3 = 3*fw0
     T hF[3];                     // (0.5*hdt)*F, the face velocity shift (src/dugks.cu:698-700)
     T Kf[NPOP];                  // 3*fw0*(c_p . F)
+    T fw2s, fw0x3s, Kfs[NPOP];   // fw2, 3*fw0, Kf divided by fw1 (fluxes are kept divided by fw1)
+    T cyuf, czuf;                // fw1*dt/dy, fw1*dt/dz
     // interpolation weights, (1-m, m) pairs in the reference's lerp form
     T ty_om, ty_m;               // transverse y, |hdt/dy|
     T tz_om, tz_m;               // transverse z, |hdt/dz|
@@ -60,6 +62,7 @@ struct StepParams {
     const T *xw;                 // [(nx+1)*19*2] x-face normal (1-m, m); face I lies between cells I, I+1 (1-based)
     const T *txw;                // [(nx+2)*19*2] transverse x (1-t, t) per column 0..nx+1
     const T *cxu;                // [nx+2] dt/dxx(i)
+    const T *cxuf;               // [nx+2] fw1*dt/dxx(i)
     // perturbation forcing (src/dugks.cu:1086-1126) as separable factors
     const T *pert_x;             // [nx+2][3]: (1-cos xx), sin xx, in-zone flag
     const T *pert_y;             // [ny+2][3]: cos(beta yy), sin(beta yy), 0
@@ -88,22 +91,36 @@ __device__ __forceinline__ void feq_pair(T eu, T base, T wr, T &fp, T &fm)
     fm = wr * (t - eu);
 }
 
-// Zeroth and first moments of 19 values in the reference's summation order
-// (src/dugks.cu:687-693): sequential over ip; the terms with c=0 add an exact
-// zero there and are skipped here.
+// Zeroth and first moments of 19 values.  Summed as balanced trees (the
+// reference sums sequentially over ip, src/dugks.cu:687-693): same values to
+// rounding, with a dependency chain of 5 additions instead of 18 -- the
+// reduced-rate FP64 pipe of GB300 is latency-bound on long chains.
 template <class T>
 __device__ __forceinline__ void moments(const T v[NPOP], T &r, T &jx, T &jy, T &jz)
 {
-    r = v[0];
-#pragma unroll
-    for (int p = 1; p < NPOP; ++p) r += v[p];
-    jx = v[1] - v[2];
-    jx += v[7]; jx -= v[8]; jx += v[9]; jx -= v[10]; jx += v[11]; jx -= v[12]; jx += v[13]; jx -= v[14];
-    jy = v[3] - v[4];
-    jy += v[7]; jy += v[8]; jy -= v[9]; jy -= v[10]; jy += v[15]; jy -= v[16]; jy += v[17]; jy -= v[18];
-    jz = v[5] - v[6];
-    jz += v[11]; jz += v[12]; jz -= v[13]; jz -= v[14]; jz += v[15]; jz += v[16]; jz -= v[17]; jz -= v[18];
+    const T a = (v[0] + v[1]) + (v[2] + v[3]);
+    const T b = (v[4] + v[5]) + (v[6] + v[7]);
+    const T c = (v[8] + v[9]) + (v[10] + v[11]);
+    const T d = (v[12] + v[13]) + (v[14] + v[15]);
+    const T e = (v[16] + v[17]) + v[18];
+    r = ((a + b) + (c + d)) + e;
+    jx = ((v[1] - v[2]) + (v[7] - v[8])) + ((v[9] - v[10]) + (v[11] - v[12])) + (v[13] - v[14]);
+    jy = ((v[3] - v[4]) + (v[7] + v[8])) + ((v[15] - v[16]) + (v[17] - v[18])) - (v[9] + v[10]);
+    jz = ((v[5] - v[6]) + (v[11] + v[12])) + ((v[15] + v[16]) - (v[17] + v[18])) - (v[13] + v[14]);
 }
+
+// 1/r: FP64 from a single-precision seed and two Newton steps (error at the
+// rounding level), cheaper than the full-precision divide on the FP64 pipe;
+// the native reciprocal for FP32.
+__device__ __forceinline__ double recip(double r)
+{
+    double x = double(__frcp_rn(float(r)));
+    double e = fma(-r, x, 1.0);
+    x = fma(x, e, x);
+    e = fma(-r, x, 1.0);
+    return fma(x, e, x);
+}
+__device__ __forceinline__ float recip(float r) { return 1.0f / r; }
 
 // All 19 equilibria for density r and velocity (u, v, w).
 template <class T>
@@ -160,7 +177,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
 
     T r, jx, jy, jz;
     moments(v, r, jx, jy, jz);
-    const T inv = T(1) / r;
+    const T inv = recip(r);
     T u = jx * inv, vv = jy * inv, w = jz * inv;
 
     T Fx, Fy, Fz;
@@ -415,20 +432,22 @@ __device__ __forceinline__ void face_grad(const StepParams<T, S> &P, const FbRea
 
 // Face equilibrium and flux (src/dugks.cu:675-709 f2ruvwh, 912-943):
 //   F_p = fw1 v_p + (fw2 + fw0 F.(c_p - u)/RT) feq_p(rho, u + hdt/2 F)
-// for the 10 populations crossing a face normal to AX, written to out[s].
+// for the 10 populations crossing a face normal to AX.  Stored divided by fw1
+// (out_s = F_p / fw1, one FMA each); the update multiplies the flux
+// differences by fw1 dt/dx instead.
 template <class T, class S, int AX>
 __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[NPOP], T out[10])
 {
     T r, jx, jy, jz;
     moments(v, r, jx, jy, jz);
-    const T inv = T(1) / r;
+    const T inv = recip(r);
     T u = jx * inv, vv = jy * inv, w = jz * inv;
-    T B = P.fw2;
+    T B = P.fw2s;
     if (P.force_on) {
         u += P.hF[0];
         vv += P.hF[1];
         w += P.hF[2];
-        B = fma(-P.fw0x3, fma(P.F[0], u, fma(P.F[1], vv, P.F[2] * w)), P.fw2);
+        B = fma(-P.fw0x3s, fma(P.F[0], u, fma(P.F[1], vv, P.F[2] * w)), P.fw2s);
     }
     const T u3 = T(3) * u, v3 = T(3) * vv, w3 = T(3) * w;
     const T base = fma(T(-1.5), fma(u, u, fma(vv, vv, w * w)), T(1));
@@ -456,7 +475,7 @@ __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[N
 #pragma unroll
     for (int s = 0; s < 10; ++s) {
         const int p = flux_pop(AX, s);
-        out[s] = fma(B + P.Kf[p], fe[p], P.fw1 * v[p]);
+        out[s] = fma(B + P.Kfs[p], fe[p], v[p]);
     }
 }
 
@@ -487,8 +506,8 @@ __device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const FbR
     face_flux<T, S, AX>(P, v, out);
 }
 
-template <class T, class S, int W, int RECON>
-__global__ void __launch_bounds__(32 * W, 1) flux_kernel(const S *__restrict__ fb, const S *f_in, S *f_out,
+template <class T, class S, int W, int RECON, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict__ fb, const S *f_in, S *f_out,
                                                        const StepParams<T, S> P, int kchunk)
 {
     __shared__ T ysh[2][W][10][32];  // +y face fluxes of every warp row (double buffer)
@@ -544,7 +563,7 @@ __global__ void __launch_bounds__(32 * W, 1) flux_kernel(const S *__restrict__ f
             if (cell) {
                 const long long c = ((long long)(k - 1) * ny + (gj - 1)) * P.pitch + (gi - 1);
                 const long long cb = R.rb(gj, k) + gi;
-                const T cxg = __ldg(P.cxu + gi);
+                const T cxg = __ldg(P.cxuf + gi);
                 const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
 #pragma unroll
                 for (int p = 0; p < NPOP; ++p) {
@@ -556,11 +575,11 @@ __global__ void __launch_bounds__(32 * W, 1) flux_kernel(const S *__restrict__ f
                     }
                     if (cy(p)) {
                         const int s = flux_slot(1, p);
-                        r = fma(cy(p) > 0 ? -P.cyu : P.cyu, fy[s] - ysh[buf][wr - 1][s][lane], r);
+                        r = fma(cy(p) > 0 ? -P.cyuf : P.cyuf, fy[s] - ysh[buf][wr - 1][s][lane], r);
                     }
                     if (cz(p)) {
                         const int s = flux_slot(2, p);
-                        r = fma(cz(p) > 0 ? -P.czu : P.czu, fzu[s] - fzd[s], r);
+                        r = fma(cz(p) > 0 ? -P.czuf : P.czuf, fzu[s] - fzd[s], r);
                     }
                     P.codec.store(f_out, p * P.ps + c, p, r);
                 }

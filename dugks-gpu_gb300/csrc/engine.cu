@@ -125,8 +125,8 @@ struct dg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     void *f = nullptr, *fb = nullptr;
-    void *tab = nullptr;          // xw | txw | cxu | pert_x | pert_y | pert_z (T-typed)
-    size_t tab_off[6] = {};
+    void *tab = nullptr;          // xw | txw | cxu | pert_x | pert_y | pert_z | cxuf (T-typed)
+    size_t tab_off[7] = {};
     double *macro = nullptr;      // rho|ux|uy|uz ghosted
     double *scratch = nullptr;    // statistics partial sums / moments partials
     size_t scratch_bytes = 0;
@@ -264,7 +264,7 @@ int build_mesh(dg_ctx *h)
 // T-typed tables (x-face normal weights, transverse x weights, dt/dxx, perturbation factors)
 template <class T, class R>
 void make_tables(const dg_ctx *h, const RefCoef<R> &c, std::vector<T> &xw, std::vector<T> &txw, std::vector<T> &cxu,
-                 std::vector<T> &px, std::vector<T> &py, std::vector<T> &pz)
+                 std::vector<T> &px, std::vector<T> &py, std::vector<T> &pz, std::vector<T> &cxuf)
 {
     const int nx = h->nx, ny = h->ny, nz = h->nz;
     const bool st = h->mesh != 0;
@@ -304,7 +304,12 @@ void make_tables(const dg_ctx *h, const RefCoef<R> &c, std::vector<T> &xw, std::
             }
         }
     }
-    for (int gi = 0; gi <= nx + 1; ++gi) cxu[gi] = st ? T(c.dt / R(h->dxx[gi])) : T(c.dt / c.dx);  // dugks.cuf:833
+    cxuf.assign(nx + 2, T(0));
+    for (int gi = 0; gi <= nx + 1; ++gi) {
+        const R cu = st ? R(c.dt / R(h->dxx[gi])) : R(c.dt / c.dx);  // dugks.cuf:833
+        cxu[gi] = T(cu);
+        cxuf[gi] = T(c.fw1 * cu);
+    }
     // perturbation forcing factors, src/dugks.cu:1101-1119
     const double pi = 3.141592653589793, pi2 = pi * 2;
     const double beta = 3, gamma = 2, zoffset = 0;
@@ -361,6 +366,14 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     P.tz_m = T(tz); P.tz_om = T(R(1 - tz));
     P.cyu = T(c.dt / c.dy);
     P.czu = T(c.dt / c.dz);
+    P.fw2s = T(c.fw2 / c.fw1);
+    P.fw0x3s = T(R(3) * c.fw0 / c.fw1);
+    for (int p = 0; p < 19; ++p) {
+        const R cf = R(dg::cx(p)) * c.F[0] + R(dg::cy(p)) * c.F[1] + R(dg::cz(p)) * c.F[2];
+        P.Kfs[p] = T(R(3) * c.fw0 * cf / c.fw1);
+    }
+    P.cyuf = T(c.fw1 * (c.dt / c.dy));
+    P.czuf = T(c.fw1 * (c.dt / c.dz));
     P.g_idx = T(R(1) / c.dx); P.g_idy = T(R(1) / c.dy); P.g_idz = T(R(1) / c.dz);
     P.g_i2dx = T(R(1) / (2 * c.dx)); P.g_i2dy = T(R(1) / (2 * c.dy)); P.g_i2dz = T(R(1) / (2 * c.dz));
     if (h->mesh != 0) {
@@ -375,6 +388,7 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     P.xw = reinterpret_cast<const T *>(base + h->tab_off[0]);
     P.txw = reinterpret_cast<const T *>(base + h->tab_off[1]);
     P.cxu = reinterpret_cast<const T *>(base + h->tab_off[2]);
+    P.cxuf = reinterpret_cast<const T *>(base + h->tab_off[6]);
     P.pert_x = reinterpret_cast<const T *>(base + h->tab_off[3]);
     P.pert_y = reinterpret_cast<const T *>(base + h->tab_off[4]);
     P.pert_z = reinterpret_cast<const T *>(base + h->tab_off[5]);
@@ -604,19 +618,19 @@ int adjoint_form(dg_ctx *h, int istep, const void *f_n, const void *lam_next, vo
 template <class T>
 int upload_tables(dg_ctx *h)
 {
-    std::vector<T> xw, txw, cxu, px, py, pz;
+    std::vector<T> xw, txw, cxu, px, py, pz, cxuf;
     if (h->prec == DG_PREC_FP64)
-        make_tables<T, double>(h, h->c64, xw, txw, cxu, px, py, pz);
+        make_tables<T, double>(h, h->c64, xw, txw, cxu, px, py, pz, cxuf);
     else
-        make_tables<T, float>(h, h->c32, xw, txw, cxu, px, py, pz);
-    const std::vector<T> *parts[6] = {&xw, &txw, &cxu, &px, &py, &pz};
+        make_tables<T, float>(h, h->c32, xw, txw, cxu, px, py, pz, cxuf);
+    const std::vector<T> *parts[7] = {&xw, &txw, &cxu, &px, &py, &pz, &cxuf};
     size_t off = 0;
-    for (int t = 0; t < 6; ++t) {
+    for (int t = 0; t < 7; ++t) {
         h->tab_off[t] = off;
         off += (parts[t]->size() * sizeof(T) + 255) / 256 * 256;
     }
     CK(cudaMalloc(&h->tab, off), "cudaMalloc (tables)");
-    for (int t = 0; t < 6; ++t)
+    for (int t = 0; t < 7; ++t)
         CK(cudaMemcpy(static_cast<char *>(h->tab) + h->tab_off[t], parts[t]->data(), parts[t]->size() * sizeof(T),
                       cudaMemcpyHostToDevice),
            "table upload");

@@ -12,11 +12,13 @@ namespace dg {
 // Flux-kernel CTA per form: W warps = W-1 rows of 32 cells plus the halo warp.
 template <class T, class S>
 struct TileCfg {
-    static constexpr int W = 9;   // 8 rows of 32 cells; ~145 registers in FP32
+    static constexpr int W = 8;     // 7 rows of 32 cells
+    static constexpr int MINB = 2;  // two CTAs per SM (<= 128 registers)
 };
 template <>
 struct TileCfg<double, double> {
-    static constexpr int W = 8;   // 7 rows; the FP64 kernel takes 255 registers at 256 threads
+    static constexpr int W = 8;     // 7 rows; the FP64 kernel takes 255 registers at 256 threads
+    static constexpr int MINB = 1;
 };
 
 template <class T, class S>

@@ -25,7 +25,7 @@ int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int occ = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0>, 32 * W, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0, TileCfg<T, S>::MINB>, 32 * W, 0);
     occ = std::max(occ, 1);
     const long long cols = (long long)((P.nx + 31) / 32) * ((P.ny + W - 2) / (W - 1));
     const long long want = 4LL * sms * occ;
@@ -40,14 +40,14 @@ template <class T, class S>
 cudaError_t Kern<T, S>::flux(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P, int recon,
                              cudaStream_t st)
 {
-    constexpr int W = TileCfg<T, S>::W;
+    constexpr int W = TileCfg<T, S>::W, MB = TileCfg<T, S>::MINB;
     const int kchunk = flux_kchunk(P);
     dim3 grid((P.nx + 31) / 32, (P.ny + W - 2) / (W - 1), (P.nz + kchunk - 1) / kchunk);
     dim3 block(32, W);
     if (recon == 1)
-        flux_kernel<T, S, W, 1><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
+        flux_kernel<T, S, W, 1, MB><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
     else
-        flux_kernel<T, S, W, 0><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
+        flux_kernel<T, S, W, 0, MB><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
     return cudaGetLastError();
 }
 
