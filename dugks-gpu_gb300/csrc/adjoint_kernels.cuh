@@ -47,10 +47,8 @@ __device__ __forceinline__ void adj_accum(AdjJac<T> &J, int p, T lam, T r, T u, 
 template <class T, class S>
 __device__ __forceinline__ T fb_at(const S *fb, const StepParams<T, S> &P, int p, int gi, int gj, int gk)
 {
-    // gi: stored column 0..nx+1 (x ghosts held by fb_ghost_kernel); gj, gk 1-based with periodic wrap
-    gj = gj == 0 ? P.ny : (gj == P.ny + 1 ? 1 : gj);
-    gk = gk == 0 ? P.nz : (gk == P.nz + 1 ? 1 : gk);
-    const long long row = ((long long)(gk - 1) * P.ny + (gj - 1)) * P.pitch_b;
+    // stored indices 0..n+1: the ghost layer written by fb_ghost_kernel holds the images
+    const long long row = ((long long)gk * (P.ny + 2) + gj) * P.pitch_b;
     return P.codec.load_nc(fb, p * P.ps_b + row + gi, p);
 }
 

@@ -2,11 +2,12 @@
 //
 // Layout in HBM: structure of arrays, one plane per population.
 //   f-tilde:         f[p*ps + ((k*ny + j)*pitch + i)]           (0-based i, j, k; interior only)
-//   f-bar-plus:     fb[p*ps_b + ((k*ny + j)*pitch_b + i + 1)]   (x ghost columns at 0 and nx+1)
-// The x ghosts of f-bar-plus are stored by fb_ghost_kernel; the y and z
-// periodic images are index wraps in the flux kernel.  Together they replace
-// the reference's extend_fb_x / extend_fb_x_wall / extend_fb_y kernels and
-// the MPI z exchange (src/dugks.cu:348-377, src/parallel.cu:185-234).
+//   f-bar-plus:     fb[p*ps_b + (((k+1)*(ny+2) + j+1)*pitch_b + i + 1)]
+//                   with one ghost layer on every side, written by
+//                   fb_ghost_kernel (periodic images, wall extrapolation);
+//                   this replaces the reference's extend_fb_x / extend_fb_x_wall /
+//                   extend_fb_y kernels and the MPI z exchange
+//                   (src/dugks.cu:348-377, src/parallel.cu:185-234).
 //
 // Kernels:
 //   fbar_kernel      stage (a), src/dugks.cu:1131-1196 (calc_fb1)
@@ -19,6 +20,7 @@
 // Template parameters: T is the arithmetic type, S the storage type of f and
 // f-bar-plus (double, float, or the 16-bit deviation codecs of storage.cuh).
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 
@@ -35,8 +37,8 @@ template <class T, class S>
 struct StepParams {
     int nx, ny, nz, pitch;
     long long ps;          // population stride of f-tilde (elements)
-    int pitch_b;           // x pitch of f-bar-plus, which stores the ghost columns 0 and nx+1
-    long long ps_b;        // population stride of f-bar-plus
+    int pitch_b;           // x pitch of f-bar-plus (>= nx+2: ghost columns 0 and nx+1 stored)
+    long long ps_b;        // population stride of f-bar-plus (>= pitch_b*(ny+2)*(nz+2))
     int periodic_x;        // 0: bounce-back walls on the two x faces
     int perturb;           // per-cell perturbation force in stage (a)
     int force_on;          // ambient force non-zero
@@ -68,6 +70,7 @@ struct StepParams {
     const T *pert_y;             // [ny+2][3]: cos(beta yy), sin(beta yy), 0
     const T *pert_z;             // [nz+2][3]: cos(gamma zz), sin(gamma zz), 0
     T pert_ax, pert_ay, pert_az, pert_FF;  // per-step amplitude prefactors
+    int *err;                    // device error flag (bit 0: a TMA pipeline wait gave up)
     Codec<T, S> codec;           // storage decode / encode constants
 };
 
@@ -169,7 +172,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     const int k = blockIdx.z;
     if (i >= P.nx) return;
     const long long c = ((long long)k * P.ny + j) * P.pitch + i;
-    const long long cb = ((long long)k * P.ny + j) * P.pitch_b + i + 1;
+    const long long cb = ((long long)(k + 1) * (P.ny + 2) + (j + 1)) * P.pitch_b + i + 1;
 
     T v[NPOP];
 #pragma unroll
@@ -211,30 +214,64 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
 }
 
 // ---------------------------------------------------------------------------
-// Ghost columns of f-bar-plus (i = 0 and nx+1 of the 1-based x index): the
-// periodic images (src/dugks.cu:1212-1229) or the linear wall extrapolation
-// (src/dugks.cu:1234-1251; stretched mesh src/fortran/channel/src/dugks.cuf:365-374).
-// The y and z images are formed by index wrapping in the flux kernel, which
-// together replaces extend_fb_y and the z halo exchange.
+// Ghost layer of f-bar-plus: every ghost cell takes its value from the
+// interior -- the periodic image in y and z (the reference's extend_fb_y and
+// z exchange, src/dugks.cu:1256-1273, src/parallel.cu:192-199) and in x the
+// periodic copy (extend_fb_x, src/dugks.cu:1212-1229) or the linear wall
+// extrapolation (extend_fb_x_wall, src/dugks.cu:1234-1251; stretched mesh
+// src/fortran/channel/src/dugks.cuf:365-374).  The result equals the
+// reference's x -> y -> z fill order.
+// Ghost cells, by group: x columns 0 and nx+1 for all stored rows and planes,
+// y rows 0 and ny+1 for interior columns and all planes, z planes 0 and nz+1
+// for the interior columns and rows.
 // ---------------------------------------------------------------------------
 template <class T, class S>
 __global__ void __launch_bounds__(256) fb_ghost_kernel(S *__restrict__ fb, const StepParams<T, S> P)
 {
-    const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;  // (k*ny + j)
-    if (row >= (long long)P.ny * P.nz) return;
-    const long long base = row * P.pitch_b;
-    const int nx = P.nx;
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const long long nxg = 2LL * (ny + 2) * (nz + 2);
+    const long long nyg = 2LL * nx * (nz + 2);
+    const long long nzg = 2LL * nx * ny;
+    long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    int gi, gj, gk;
+    if (q < nxg) {
+        gi = (q & 1) ? nx + 1 : 0;
+        q >>= 1;
+        gj = int(q % (ny + 2));
+        gk = int(q / (ny + 2));
+    } else if ((q -= nxg) < nyg) {
+        gj = (q & 1) ? ny + 1 : 0;
+        q >>= 1;
+        gi = int(q % nx) + 1;
+        gk = int(q / nx);
+    } else if ((q -= nyg) < nzg) {
+        gk = (q & 1) ? nz + 1 : 0;
+        q >>= 1;
+        gi = int(q % nx) + 1;
+        gj = int(q / nx) + 1;
+    } else {
+        return;
+    }
+    // periodic images in y and z
+    const int sj = gj == 0 ? ny : (gj == ny + 1 ? 1 : gj);
+    const int sk = gk == 0 ? nz : (gk == nz + 1 ? 1 : gk);
+    const long long dst = ((long long)gk * (ny + 2) + gj) * P.pitch_b + gi;
+    const long long row = ((long long)sk * (ny + 2) + sj) * P.pitch_b;
+    if (gi >= 1 && gi <= nx) {
 #pragma unroll
-    for (int p = 0; p < NPOP; ++p) {
-        S *r = fb + p * P.ps_b + base;
-        if (P.periodic_x) {
-            r[0] = r[nx];
-            r[nx + 1] = r[1];
-        } else {
-            const T a0 = P.codec.load(r, 1, p), a1 = P.codec.load(r, 2, p);
-            const T b0 = P.codec.load(r, nx, p), b1 = P.codec.load(r, nx - 1, p);
-            P.codec.store(r, 0, p, P.q0 * a0 + (T(1) - P.q0) * a1);
-            P.codec.store(r, nx + 1, p, P.q1 * b0 + (T(1) - P.q1) * b1);
+        for (int p = 0; p < NPOP; ++p) fb[p * P.ps_b + dst] = fb[p * P.ps_b + row + gi];
+    } else if (P.periodic_x) {
+        const int si = gi == 0 ? nx : 1;
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) fb[p * P.ps_b + dst] = fb[p * P.ps_b + row + si];
+    } else {
+        const int a = gi == 0 ? 1 : nx, b = gi == 0 ? 2 : nx - 1;
+        const T q0 = gi == 0 ? P.q0 : P.q1;
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) {
+            const T va = P.codec.load(fb, p * P.ps_b + row + a, p);
+            const T vb = P.codec.load(fb, p * P.ps_b + row + b, p);
+            P.codec.store(fb, p * P.ps_b + dst, p, q0 * va + (T(1) - q0) * vb);
         }
     }
 }
@@ -252,6 +289,7 @@ __global__ void __launch_bounds__(256) fb_ghost_kernel(S *__restrict__ fb, const
 // L1 (no shared-memory staging); its ghost columns are stored by
 // fb_ghost_kernel and its y / z images are index wraps.
 // ---------------------------------------------------------------------------
+// f-bar-plus through L1: rows and planes are stored indices 0..n+1 (ghosts included)
 template <class T, class S>
 struct FbRead {
     const S *fb;
@@ -260,7 +298,7 @@ struct FbRead {
     const Codec<T, S> &codec;
     __device__ __forceinline__ long long rb(int j, int k) const
     {
-        return ((long long)(k - 1) * ny + (j - 1)) * pitch;
+        return ((long long)k * (ny + 2) + j) * pitch;
     }
     __device__ __forceinline__ T operator()(int p, long long row, int col) const
     {
@@ -268,29 +306,22 @@ struct FbRead {
     }
 };
 
-__device__ __forceinline__ int wrap1(int j, int n)
-{
-    // 1-based periodic index for j in [0, 2n]; values beyond clamp (unused lanes)
-    j = j < 1 ? j + n : (j > n ? j - n : j);
-    return j < 1 ? 1 : (j > n ? n : j);
-}
-
 // 19 reconstructed values of one face, trilinear characteristic interpolation
 // (src/dugks.cu:756-906) in the reference's x -> y -> z lerp order:
 //   AX=0: face I between columns I and I+1 (I = 0: anchor column 1, other 0)
 //   AX=1: face J between rows J and J+1 at column i
 //   AX=2: face K between planes K and K+1 at column i
-template <class T, class S, int AX>
-__device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const FbRead<T, S> &R, int i, int j, int k,
-                                         T v[NPOP])
+template <class T, class S, int AX, class RD>
+__device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R, int i, int j, int k, T v[NPOP])
 {
-    const int ny = P.ny, nz = P.nz;
-    const int jm = wrap1(j - 1, ny), jp = wrap1(j + 1, ny), jc = wrap1(j, ny);
-    const int km = wrap1(k - 1, nz), kp = wrap1(k + 1, nz), kc = wrap1(k, nz);
+    using RI = decltype(R.rb(0, 0));
+    // j, k are stored indices (ghost rows / planes 0 and n+1 hold the periodic images)
+    const int jm = j - 1, jp = j + 1, jc = j;
+    const int km = k - 1, kp = k + 1, kc = k;
     if (AX == 0) {
         const int A = i == 0 ? 1 : i, B = i == 0 ? 0 : i + 1;
         const T *xw = P.xw + (size_t)i * 38;
-        const long long r00 = R.rb(jc, kc);
+        const RI r00 = R.rb(jc, kc);
         v[0] = T(0.5) * (R(0, r00, A) + R(0, r00, B));
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
@@ -301,15 +332,15 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const FbRead
             const T x00 = lerp2(om, m, R(p, r00, A), R(p, r00, B));
             T y00 = x00;
             if (ay) {
-                const long long r10 = R.rb(jt, kc);
+                const RI r10 = R.rb(jt, kc);
                 y00 = lerp2(P.ty_om, P.ty_m, x00, lerp2(om, m, R(p, r10, A), R(p, r10, B)));
             }
             if (az) {
-                const long long r01 = R.rb(jc, kt);
+                const RI r01 = R.rb(jc, kt);
                 const T x10 = lerp2(om, m, R(p, r01, A), R(p, r01, B));
                 T y11 = x10;
                 if (ay) {
-                    const long long r11 = R.rb(jt, kt);
+                    const RI r11 = R.rb(jt, kt);
                     y11 = lerp2(P.ty_om, P.ty_m, x10, lerp2(om, m, R(p, r11, A), R(p, r11, B)));
                 }
                 v[p] = lerp2(P.tz_om, P.tz_m, y00, y11);
@@ -319,7 +350,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const FbRead
         }
     } else if (AX == 1) {
         // rows j (anchor) and j+1 (other); transverse x to column i - cx, z to plane k - cz
-        const long long rA = R.rb(jc, kc), rB = R.rb(jp, kc);
+        const RI rA = R.rb(jc, kc), rB = R.rb(jp, kc);
         v[0] = T(0.5) * (R(0, rA, i) + R(0, rB, i));
         const T *tw = P.txw + (size_t)i * 38;
 #pragma unroll
@@ -336,7 +367,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const FbRead
             }
             const T y00 = lerp2(P.yn_om[p], P.yn_m[p], x00, x01);
             if (az) {
-                const long long sA = R.rb(jc, kt), sB = R.rb(jp, kt);
+                const RI sA = R.rb(jc, kt), sB = R.rb(jp, kt);
                 T x10 = R(p, sA, i), x11 = R(p, sB, i);
                 if (ax) {
                     x10 = lerp2(txo, txm, x10, R(p, sA, io));
@@ -349,7 +380,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const FbRead
         }
     } else {
         // planes k (anchor) and k+1 (other); transverse x to i - cx, y to row j - cy
-        const long long rA = R.rb(jc, kc), rB = R.rb(jc, kp);
+        const RI rA = R.rb(jc, kc), rB = R.rb(jc, kp);
         v[0] = T(0.5) * (R(0, rA, i) + R(0, rB, i));
         const T *tw = P.txw + (size_t)i * 38;
 #pragma unroll
@@ -366,7 +397,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const FbRead
             }
             T y00 = x00, y11 = x10;
             if (ay) {
-                const long long sA = R.rb(jt, kc), sB = R.rb(jt, kp);
+                const RI sA = R.rb(jt, kc), sB = R.rb(jt, kp);
                 T x01 = R(p, sA, i), x11 = R(p, sB, i);
                 if (ax) {
                     x01 = lerp2(txo, txm, x01, R(p, sA, io));
@@ -384,41 +415,40 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const FbRead
 // f_face = mean - hdt (c . grad), src/dugks.cu:459-583 (calc_fx): normal
 // gradient across the face, transverse gradients of face-averaged neighbours
 // over two cells.  Uniform mesh.
-template <class T, class S, int AX>
-__device__ __forceinline__ void face_grad(const StepParams<T, S> &P, const FbRead<T, S> &R, int i, int j, int k,
-                                          T v[NPOP])
+template <class T, class S, int AX, class RD>
+__device__ __forceinline__ void face_grad(const StepParams<T, S> &P, const RD &R, int i, int j, int k, T v[NPOP])
 {
-    const int ny = P.ny, nz = P.nz;
-    const int jm = wrap1(j - 1, ny), jp = wrap1(j + 1, ny), jc = wrap1(j, ny);
-    const int km = wrap1(k - 1, nz), kp = wrap1(k + 1, nz), kc = wrap1(k, nz);
+    using RI = decltype(R.rb(0, 0));
+    const int jm = j - 1, jp = j + 1, jc = j;
+    const int km = k - 1, kp = k + 1, kc = k;
     const T h = P.hdt;
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
         T temp, gx, gy, gz;
         if (AX == 0) {
             const int L = i, Rr = i + 1;  // left / right column of face I = i
-            const long long r = R.rb(jc, kc);
+            const RI r = R.rb(jc, kc);
             const T a = R(p, r, Rr), b = R(p, r, L);
             temp = T(0.5) * (a + b);
             gx = (a - b) * P.g_idx;
-            const long long ru = R.rb(jp, kc), rd = R.rb(jm, kc);
+            const RI ru = R.rb(jp, kc), rd = R.rb(jm, kc);
             gy = (T(0.5) * (R(p, ru, L) + R(p, ru, Rr)) - T(0.5) * (R(p, rd, L) + R(p, rd, Rr))) * P.g_i2dy;
-            const long long rt = R.rb(jc, kp), rbo = R.rb(jc, km);
+            const RI rt = R.rb(jc, kp), rbo = R.rb(jc, km);
             gz = (T(0.5) * (R(p, rt, L) + R(p, rt, Rr)) - T(0.5) * (R(p, rbo, L) + R(p, rbo, Rr))) * P.g_i2dz;
         } else if (AX == 1) {
-            const long long rD = R.rb(jc, kc), rU = R.rb(jp, kc);
+            const RI rD = R.rb(jc, kc), rU = R.rb(jp, kc);
             const T a = R(p, rU, i), b = R(p, rD, i);
             temp = T(0.5) * (a + b);
             gx = (T(0.5) * (R(p, rD, i + 1) + R(p, rU, i + 1)) - T(0.5) * (R(p, rD, i - 1) + R(p, rU, i - 1))) * P.g_i2dx;
             gy = (a - b) * P.g_idy;
-            const long long tD = R.rb(jc, kp), tU = R.rb(jp, kp), bD = R.rb(jc, km), bU = R.rb(jp, km);
+            const RI tD = R.rb(jc, kp), tU = R.rb(jp, kp), bD = R.rb(jc, km), bU = R.rb(jp, km);
             gz = (T(0.5) * (R(p, tD, i) + R(p, tU, i)) - T(0.5) * (R(p, bD, i) + R(p, bU, i))) * P.g_i2dz;
         } else {
-            const long long rB = R.rb(jc, kc), rT = R.rb(jc, kp);
+            const RI rB = R.rb(jc, kc), rT = R.rb(jc, kp);
             const T a = R(p, rT, i), b = R(p, rB, i);
             temp = T(0.5) * (a + b);
             gx = (T(0.5) * (R(p, rB, i + 1) + R(p, rT, i + 1)) - T(0.5) * (R(p, rB, i - 1) + R(p, rT, i - 1))) * P.g_i2dx;
-            const long long uB = R.rb(jp, kc), uT = R.rb(jp, kp), dB = R.rb(jm, kc), dT = R.rb(jm, kp);
+            const RI uB = R.rb(jp, kc), uT = R.rb(jp, kp), dB = R.rb(jm, kc), dT = R.rb(jm, kp);
             gy = (T(0.5) * (R(p, uB, i) + R(p, uT, i)) - T(0.5) * (R(p, dB, i) + R(p, dT, i))) * P.g_i2dy;
             gz = (a - b) * P.g_idz;
         }
@@ -493,9 +523,8 @@ __device__ __forceinline__ void bounce_back(T v[NPOP], bool lo, bool hi)
 }
 
 // Fluxes of one face: reconstruction + bounce-back + face equilibrium.
-template <class T, class S, int AX, int RECON>
-__device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const FbRead<T, S> &R, int i, int j, int k,
-                                            T out[10])
+template <class T, class S, int AX, int RECON, class RD>
+__device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const RD &R, int i, int j, int k, T out[10])
 {
     T v[NPOP];
     if (RECON == 0)
@@ -589,6 +618,186 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict_
         }
         buf ^= 1;
     }
+}
+
+// ---------------------------------------------------------------------------
+// TMA-fed variant of flux_kernel.  The CTA's window of f-bar-plus -- columns
+// i0-1 .. i0+32, rows j0-1 .. j0+W-1, all 19 populations of one plane -- is
+// one 4-D tile of the ghosted f-bar-plus tensor (x, y, z, population); it
+// arrives in a 4-stage shared-memory ring through cp.async.bulk.tensor with
+// mbarrier completion, two planes ahead of use.  The faces read the ring
+// instead of global memory; everything else is flux_kernel.
+// ---------------------------------------------------------------------------
+template <class S>
+struct TmaTile {
+    // tile width in elements: >= 34 columns, row bytes a multiple of 16
+    static constexpr int BXT = sizeof(S) == 8 ? 34 : (sizeof(S) == 4 ? 36 : 40);
+};
+
+template <class T, class S, int W>
+struct SmemRead {
+    static constexpr int BXT = TmaTile<S>::BXT, RH = W + 1, POPS = BXT * RH;
+    static constexpr int STAGE_BYTES = ((NPOP * POPS * int(sizeof(S))) + 127) / 128 * 128;
+    static constexpr int STAGE = STAGE_BYTES / int(sizeof(S));
+    const S *ring;
+    int i0m1, j0m1;
+    const Codec<T, S> &codec;
+    __device__ __forceinline__ int rb(int j, int k) const { return (k & 3) * STAGE + (j - j0m1) * BXT - i0m1; }
+    __device__ __forceinline__ T operator()(int p, int row, int col) const
+    {
+        return codec.load_s(ring, p * POPS + row + col, p);
+    }
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+    return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+
+// bounded wait on an mbarrier phase; false if it never completed
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+{
+    for (int it = 0; it < (1 << 22); ++it) {
+        unsigned ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+template <class T, class S, int W, int RECON, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                                 const S *f_in, S *f_out,
+                                                                 const StepParams<T, S> P, int kchunk)
+{
+    using RD = SmemRead<T, S, W>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    S *ring = reinterpret_cast<S *>(smem);
+    T(*ysh)[W][10][32] = reinterpret_cast<T(*)[W][10][32]>(smem + 4 * RD::STAGE_BYTES);
+    T(*xsh)[W][10] = reinterpret_cast<T(*)[W][10]>(smem + 4 * RD::STAGE_BYTES + 2 * W * 10 * 32 * sizeof(T));
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(
+        smem + 4 * RD::STAGE_BYTES + 2 * W * 10 * 32 * sizeof(T) + 2 * W * 10 * sizeof(T));
+    constexpr unsigned TILE_BYTES = unsigned(NPOP * RD::POPS * sizeof(S));
+
+    const int lane = threadIdx.x, wr = threadIdx.y, tid = wr * 32 + lane;
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const int i0 = blockIdx.x * 32 + 1;
+    const int j0 = blockIdx.y * (W - 1) + 1;
+    const int kb = blockIdx.z * kchunk + 1;
+    const int ke = min(kb + kchunk, nz + 1);
+    if (kb >= ke) return;
+    const RD R{ring, i0 - 1, j0 - 1, P.codec};
+
+    if (tid == 0) {
+        for (int s = 0; s < 4; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar + s)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int g) {  // stored plane g -> stage g & 3
+        if (tid == 0 && g <= ke) {
+            const unsigned bar = smem_u32(mbar + (g & 3));
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(TILE_BYTES)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+                "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(ring + (g & 3) * RD::STAGE)),
+                "l"(reinterpret_cast<unsigned long long>(&tmap)), "r"(i0 - 1), "r"(j0 - 1), "r"(g), "r"(0), "r"(bar)
+                : "memory");
+        }
+    };
+    unsigned phase = 0;  // bit s: parity of the next completion of stage s
+    auto wait = [&](int g) {
+        const int s = g & 3;
+        if (!mbar_wait(smem_u32(mbar + s), (phase >> s) & 1u)) atomicOr(P.err, 1);
+        phase ^= 1u << s;
+    };
+
+    const int gi = i0 + lane;
+    const int gj = j0 + wr - 1;
+    const bool cell = wr >= 1 && gi <= nx && gj <= ny;
+    const int ci = min(gi, nx);
+    const int cj = wr >= 1 ? min(gj, ny) : 1;
+    const int hj = j0 + lane;
+    const bool hx = wr == 0 && lane < W - 1 && hj <= ny;
+
+    for (int g = kb - 1; g <= kb + 2; ++g) issue(g);
+    T fzd[10], fzu[10], fx[10], fy[10];
+    int buf = 0;
+    wait(kb - 1);
+    wait(kb);
+    if (wr >= 1) face_fluxes<T, S, 2, RECON>(P, R, ci, cj, kb - 1, fzd);
+    for (int k = kb; k < ke; ++k) {
+        wait(k + 1);
+        if (wr >= 1) {
+            face_fluxes<T, S, 0, RECON>(P, R, ci, cj, k, fx);
+            face_fluxes<T, S, 1, RECON>(P, R, ci, cj, k, fy);
+            face_fluxes<T, S, 2, RECON>(P, R, ci, cj, k, fzu);
+#pragma unroll
+            for (int s = 0; s < 10; ++s) ysh[buf][wr][s][lane] = fy[s];
+        } else {
+            face_fluxes<T, S, 1, RECON>(P, R, ci, j0 - 1, k, fy);
+#pragma unroll
+            for (int s = 0; s < 10; ++s) ysh[buf][0][s][lane] = fy[s];
+            if (hx) {
+                T hxf[10];
+                face_fluxes<T, S, 0, RECON>(P, R, i0 - 1, hj, k, hxf);
+#pragma unroll
+                for (int s = 0; s < 10; ++s) xsh[buf][lane + 1][s] = hxf[s];
+            }
+        }
+        __syncthreads();
+        issue(k + 3);  // plane k-1 (same stage) is no longer read
+        if (wr >= 1) {
+            T fxl[10];
+#pragma unroll
+            for (int s = 0; s < 10; ++s) {
+                const T up = __shfl_up_sync(0xffffffffu, fx[s], 1);
+                fxl[s] = lane == 0 ? xsh[buf][wr][s] : up;
+            }
+            if (cell) {
+                const long long c = ((long long)(k - 1) * ny + (gj - 1)) * P.pitch + (gi - 1);
+                const int cb = R.rb(gj, k) + gi;
+                const T cxg = __ldg(P.cxuf + gi);
+                const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
+#pragma unroll
+                for (int p = 0; p < NPOP; ++p) {
+                    const T fo = P.codec.load(f_in, p * P.ps + c, p);
+                    T r = fma(R(p, cb, 0), c43, -(fo * c13));
+                    if (cx(p)) {
+                        const int s = flux_slot(0, p);
+                        r = fma(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s], r);
+                    }
+                    if (cy(p)) {
+                        const int s = flux_slot(1, p);
+                        r = fma(cy(p) > 0 ? -P.cyuf : P.cyuf, fy[s] - ysh[buf][wr - 1][s][lane], r);
+                    }
+                    if (cz(p)) {
+                        const int s = flux_slot(2, p);
+                        r = fma(cz(p) > 0 ? -P.czuf : P.czuf, fzu[s] - fzd[s], r);
+                    }
+                    P.codec.store(f_out, p * P.ps + c, p, r);
+                }
+            }
+#pragma unroll
+            for (int s = 0; s < 10; ++s) fzd[s] = fzu[s];
+        }
+        buf ^= 1;
+    }
+    // every plane issued (g <= ke) has been waited for: no bulk copy is left in flight
+}
+
+template <class T, class S, int W>
+constexpr size_t flux_tma_smem_bytes()
+{
+    using RD = SmemRead<T, S, W>;
+    return 4 * size_t(RD::STAGE_BYTES) + 2 * W * 10 * 32 * sizeof(T) + 2 * W * 10 * sizeof(T) + 4 * 8;
 }
 
 // ---------------------------------------------------------------------------

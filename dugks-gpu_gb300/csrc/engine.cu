@@ -132,6 +132,9 @@ struct dg_ctx {
     size_t scratch_bytes = 0;
     void *adj = nullptr;          // per-face adjoint scratch (allocated on first dg_adjoint_step)
     double *acc = nullptr;        // running sums of the per-x statistics (dg_stats_accumulate)
+    int *dev_err = nullptr;       // device error flag written by the kernels (TMA wait time-outs)
+    CUtensorMap tmap;             // f-bar-plus tensor map of the TMA flux kernel (64-byte aligned type)
+    bool have_tmap = false;
     long long acc_count = 0;
     bool macro_valid = false;
 
@@ -144,6 +147,7 @@ struct dg_ctx {
         if (scratch) cudaFree(scratch);
         if (adj) cudaFree(adj);
         if (acc) cudaFree(acc);
+        if (dev_err) cudaFree(dev_err);
     }
     int fail(int code, const std::string &msg)
     {
@@ -389,6 +393,7 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     P.txw = reinterpret_cast<const T *>(base + h->tab_off[1]);
     P.cxu = reinterpret_cast<const T *>(base + h->tab_off[2]);
     P.cxuf = reinterpret_cast<const T *>(base + h->tab_off[6]);
+    P.err = h->dev_err;
     P.pert_x = reinterpret_cast<const T *>(base + h->tab_off[3]);
     P.pert_y = reinterpret_cast<const T *>(base + h->tab_off[4]);
     P.pert_z = reinterpret_cast<const T *>(base + h->tab_off[5]);
@@ -456,7 +461,7 @@ int step_form(dg_ctx *h, int istep0, int n, cudaEvent_t *ev)
         if (h->perturb && s > 0) P = params_for<T, S>(h, istep0 + s);
         CK(K::fbar(f, fb, P, h->stream), "stage (a) launch");
         if (ev) CK(cudaEventRecord(ev[2 * s + 1], h->stream), "event record");
-        CK(K::flux(fb, f, f, P, h->recon, h->stream), "flux launch");
+        CK(K::flux(fb, f, f, P, h->recon, h->have_tmap ? &h->tmap : nullptr, h->stream), "flux launch");
         if (ev) CK(cudaEventRecord(ev[2 * s + 2], h->stream), "event record");
     }
     h->macro_valid = false;
@@ -637,6 +642,17 @@ int upload_tables(dg_ctx *h)
     return DG_OK;
 }
 
+template <class T, class S>
+int make_tmap_form(dg_ctx *h)
+{
+    using K = Kern<T, S>;
+    if (!K::uses_tma()) return DG_OK;
+    const int r = K::make_tmap(static_cast<const S *>(h->fb), h->nx, h->ny, h->nz, h->pitch_b, h->ps_b, &h->tmap);
+    if (r) return h->fail(DG_ERR_CUDA, "cuTensorMapEncodeTiled failed for the f-bar-plus tensor map (" + std::to_string(r) + ")");
+    h->have_tmap = true;
+    return DG_OK;
+}
+
 int allocate(dg_ctx *h)
 {
     const size_t sb = storage_bytes(h->prec);
@@ -646,14 +662,18 @@ int allocate(dg_ctx *h)
     const long long a256 = 256 / (long long)sb;
     h->ps = (plane + a256 - 1) / a256 * a256;
     h->pitch_b = (h->nx + 2 + align - 1) / align * align;
-    const long long plane_b = (long long)h->pitch_b * h->ny * h->nz;
+    const long long plane_b = (long long)h->pitch_b * (h->ny + 2) * (h->nz + 2);
     h->ps_b = (plane_b + a256 - 1) / a256 * a256;
     const size_t bytes = size_t(h->ps) * 19 * sb, bytes_b = size_t(h->ps_b) * 19 * sb;
     CK(cudaMalloc(&h->f, bytes), "cudaMalloc (f)");
     CK(cudaMalloc(&h->fb, bytes_b), "cudaMalloc (fb)");
     CK(cudaMemset(h->f, 0, bytes), "cudaMemset (f)");
     CK(cudaMemset(h->fb, 0, bytes_b), "cudaMemset (fb)");
-    return h->prec == DG_PREC_FP64 ? upload_tables<double>(h) : upload_tables<float>(h);
+    CK(cudaMalloc(&h->dev_err, sizeof(int)), "cudaMalloc (error flag)");
+    CK(cudaMemset(h->dev_err, 0, sizeof(int)), "cudaMemset (error flag)");
+    int rc = h->prec == DG_PREC_FP64 ? upload_tables<double>(h) : upload_tables<float>(h);
+    if (rc) return rc;
+    return DISPATCH(h, make_tmap_form);
 }
 
 // host equilibrium, src/dugks.cu:304-309
@@ -1003,6 +1023,12 @@ int dg_sync(dg_t *h)
     if (!h) return DG_ERR_ARG;
     CK(cudaStreamSynchronize(h->stream), "stream synchronize");
     CK(cudaGetLastError(), "pending CUDA error");
+    int flag = 0;
+    CK(cudaMemcpy(&flag, h->dev_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag read");
+    if (flag) {
+        cudaMemset(h->dev_err, 0, sizeof(int));
+        return h->fail(DG_ERR_CUDA, "a TMA pipeline wait in the flux kernel timed out");
+    }
     return DG_OK;
 }
 

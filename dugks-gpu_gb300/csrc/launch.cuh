@@ -10,15 +10,25 @@
 namespace dg {
 
 // Flux-kernel CTA per form: W warps = W-1 rows of 32 cells plus the halo warp.
+// TMA selects flux_tma_kernel (f-bar-plus through a TMA-fed shared-memory ring)
+// instead of flux_kernel (f-bar-plus through L1).
 template <class T, class S>
 struct TileCfg {
-    static constexpr int W = 8;     // 7 rows of 32 cells
-    static constexpr int MINB = 2;  // two CTAs per SM (<= 128 registers)
+    static constexpr int W = 8;       // 7 rows of 32 cells
+    static constexpr int MINB = 2;    // two CTAs per SM (<= 128 registers)
+    static constexpr bool TMA = true; // 4 x 13.7 KB planes per CTA for 16-bit storage
+};
+template <>
+struct TileCfg<float, float> {
+    static constexpr int W = 7;       // 6 rows: 4 x 21.9 KB planes, two CTAs per SM
+    static constexpr int MINB = 2;
+    static constexpr bool TMA = true;
 };
 template <>
 struct TileCfg<double, double> {
-    static constexpr int W = 8;     // 7 rows; the FP64 kernel takes 255 registers at 256 threads
+    static constexpr int W = 8;       // 7 rows; the FP64 kernel takes 255 registers at 256 threads
     static constexpr int MINB = 1;
+    static constexpr bool TMA = false;
 };
 
 template <class T, class S>
@@ -26,9 +36,13 @@ struct Kern {
     // stage (a) and the x ghost columns of f-bar-plus
     static cudaError_t fbar(const S *f, S *fb, const StepParams<T, S> &P, cudaStream_t st);
     // stages (b)-(e); recon 0 trilinear, 1 central-difference gradient.
-    // f_in may equal f_out (in-place update, as the reference)
+    // f_in may equal f_out (in-place update, as the reference).  tmap: the
+    // f-bar-plus tensor map of make_tmap (used when TileCfg::TMA).
     static cudaError_t flux(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P, int recon,
-                            cudaStream_t st);
+                            const CUtensorMap *tmap, cudaStream_t st);
+    static bool uses_tma() { return TileCfg<T, S>::TMA; }
+    // 4-D tensor map (x, y, z, population) over the ghosted f-bar-plus array
+    static int make_tmap(const S *fb, int nx, int ny, int nz, int pitch_b, long long ps_b, CUtensorMap *out);
     static cudaError_t macro(const S *f, const StepParams<T, S> &P, double hdt, const double F[3], double *rho,
                              double *ux, double *uy, double *uz, cudaStream_t st);
     static cudaError_t aos_to_soa(const double *src, S *dst, const StepParams<T, S> &P, cudaStream_t st);

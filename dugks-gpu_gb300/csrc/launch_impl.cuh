@@ -2,6 +2,7 @@
 #pragma once
 #include <algorithm>
 #include <type_traits>
+#include <cudaTypedefs.h>
 #include "launch.cuh"
 
 namespace dg {
@@ -12,20 +13,24 @@ cudaError_t Kern<T, S>::fbar(const S *f, S *fb, const StepParams<T, S> &P, cudaS
     const int bx = P.nx >= 128 ? 128 : ((P.nx + 31) / 32) * 32;
     dim3 grid((P.nx + bx - 1) / bx, P.ny, P.nz);
     fbar_kernel<T, S><<<grid, bx, 0, st>>>(f, fb, P);
-    const long long rows = (long long)P.ny * P.nz;
-    fb_ghost_kernel<T, S><<<unsigned((rows + 255) / 256), 256, 0, st>>>(fb, P);
+    const long long ghosts = 2LL * (P.ny + 2) * (P.nz + 2) + 2LL * P.nx * (P.nz + 2) + 2LL * P.nx * P.ny;
+    fb_ghost_kernel<T, S><<<unsigned((ghosts + 255) / 256), 256, 0, st>>>(fb, P);
     return cudaGetLastError();
 }
 
 template <class T, class S>
 int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
 {
-    constexpr int W = TileCfg<T, S>::W;
+    constexpr int W = TileCfg<T, S>::W, MB = TileCfg<T, S>::MINB;
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int occ = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0, TileCfg<T, S>::MINB>, 32 * W, 0);
+    if (TileCfg<T, S>::TMA)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_tma_kernel<T, S, W, 0, MB>, 32 * W,
+                                                      flux_tma_smem_bytes<T, S, W>());
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0, MB>, 32 * W, 0);
     occ = std::max(occ, 1);
     const long long cols = (long long)((P.nx + 31) / 32) * ((P.ny + W - 2) / (W - 1));
     const long long want = 4LL * sms * occ;
@@ -38,12 +43,32 @@ int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
 
 template <class T, class S>
 cudaError_t Kern<T, S>::flux(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P, int recon,
-                             cudaStream_t st)
+                             const CUtensorMap *tmap, cudaStream_t st)
 {
     constexpr int W = TileCfg<T, S>::W, MB = TileCfg<T, S>::MINB;
+    static bool attr_set = false;
+    if (TileCfg<T, S>::TMA && !attr_set) {
+        const int bytes = int(flux_tma_smem_bytes<T, S, W>());
+        cudaError_t e = cudaFuncSetAttribute(flux_tma_kernel<T, S, W, 0, MB>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(flux_tma_kernel<T, S, W, 1, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     bytes);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
     const int kchunk = flux_kchunk(P);
     dim3 grid((P.nx + 31) / 32, (P.ny + W - 2) / (W - 1), (P.nz + kchunk - 1) / kchunk);
     dim3 block(32, W);
+    if (TileCfg<T, S>::TMA) {
+        if (!tmap) return cudaErrorInvalidValue;
+        const size_t bytes = flux_tma_smem_bytes<T, S, W>();
+        if (recon == 1)
+            flux_tma_kernel<T, S, W, 1, MB><<<grid, block, bytes, st>>>(*tmap, f_in, f_out, P, kchunk);
+        else
+            flux_tma_kernel<T, S, W, 0, MB><<<grid, block, bytes, st>>>(*tmap, f_in, f_out, P, kchunk);
+        return cudaGetLastError();
+    }
     if (recon == 1)
         flux_kernel<T, S, W, 1, MB><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
     else
@@ -117,6 +142,35 @@ cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_o
         adj_gather_kernel<T, S><<<grid, 128, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, P);
         return cudaGetLastError();
     }
+}
+
+template <class T, class S>
+int Kern<T, S>::make_tmap(const S *fb, int nx, int ny, int nz, int pitch_b, long long ps_b, CUtensorMap *out)
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn)
+            return -1;
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    constexpr int W = TileCfg<T, S>::W;
+    const CUtensorMapDataType dt = sizeof(S) == 8   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
+                                   : sizeof(S) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                   : std::is_same<S, __half>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                                                    : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
+    const cuuint64_t dims[4] = {cuuint64_t(nx + 2), cuuint64_t(ny + 2), cuuint64_t(nz + 2), cuuint64_t(NPOP)};
+    const cuuint64_t strides[3] = {cuuint64_t(pitch_b) * sizeof(S), cuuint64_t(pitch_b) * (ny + 2) * sizeof(S),
+                                   cuuint64_t(ps_b) * sizeof(S)};
+    const cuuint32_t box[4] = {cuuint32_t(TmaTile<S>::BXT), cuuint32_t(W + 1), 1u, cuuint32_t(NPOP)};
+    const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
+    const CUresult r = encode(out, dt, 4, const_cast<S *>(fb), dims, strides, box, estr,
+                              CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? 0 : int(r);
 }
 
 }  // namespace dg

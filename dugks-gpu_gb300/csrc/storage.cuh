@@ -16,6 +16,7 @@ template <class T, class S>
 struct Codec {
     __device__ __forceinline__ T load(const S *a, long long idx, int) const { return T(a[idx]); }
     __device__ __forceinline__ T load_nc(const S *a, long long idx, int) const { return T(__ldg(a + idx)); }
+    __device__ __forceinline__ T load_s(const S *a, int idx, int) const { return T(a[idx]); }
     __device__ __forceinline__ void store(S *a, long long idx, int, T v) const { a[idx] = S(v); }
     static constexpr bool deviation = false;
 };
@@ -38,6 +39,10 @@ struct Codec<float, __half> : DevCodec<__half> {
     {
         return fmaf(s[p], __half2float(__ldg(a + idx)), w[p]);
     }
+    __device__ __forceinline__ float load_s(const __half *a, int idx, int p) const
+    {
+        return fmaf(s[p], __half2float(a[idx]), w[p]);
+    }
     __device__ __forceinline__ void store(__half *a, long long idx, int p, float v) const
     {
         a[idx] = __float2half_rn((v - w[p]) * is[p]);
@@ -53,6 +58,10 @@ struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
     __device__ __forceinline__ float load_nc(const __nv_bfloat16 *a, long long idx, int p) const
     {
         return fmaf(s[p], __bfloat162float(__ldg(a + idx)), w[p]);
+    }
+    __device__ __forceinline__ float load_s(const __nv_bfloat16 *a, int idx, int p) const
+    {
+        return fmaf(s[p], __bfloat162float(a[idx]), w[p]);
     }
     __device__ __forceinline__ void store(__nv_bfloat16 *a, long long idx, int p, float v) const
     {

@@ -88,3 +88,34 @@ def test_gradient_option_matches_reference():
     eng.set_state(f0)
     eng.run(1, 5)
     assert rel_err(eng.get_state(), pyoracle.interior(ref)) <= 1e-12
+
+
+# Laminar channel of the benchmark configurations in the reference orientation:
+# 64 (walls) x 32 x 32 cells, dx = 1, force along z, centreline velocity 0.1,
+# Re_c = u_c H / nu = 100 with H = 32 (nu = 0.032), CFL 0.5, rest start f = w_p.
+C1 = dict(nx=64, ny=32, nz=32, xwidth=64, ywidth=32, zwidth=32, periods_x=0, CFL=0.5, visc=0.032,
+          ambient_fz=6.25e-6)
+
+
+def _rest_state(nx, ny, nz):
+    from seeded import W
+    return np.ascontiguousarray(np.broadcast_to(W, (nz, ny, nx, 19)))
+
+
+@pytest.mark.slow
+def test_laminar_channel_matches_reference_over_1e4_steps():
+    """FP64 engine vs the reference's kernels: <= 1e-12 relative in f-tilde after
+    1, 100, 1000 and 10^4 steps (the spec parity bound)."""
+    _need_ref()
+    f0 = _rest_state(64, 32, 32)
+    ref = pyoracle.to_ghosted(f0)
+    eng = pydugks.Engine(pydugks.make_config(**C1))
+    eng.set_state(f0)
+    done = 0
+    for upto in (1, 100, 1000, 10000):
+        pyoracle.ref_run(ref, **_ref_args(C1), istep0=done + 1, nsteps=upto - done, prec=0)
+        eng.run(done + 1, upto - done)
+        done = upto
+        err = rel_err(eng.get_state(), pyoracle.interior(ref))
+        print(f"laminar channel, {upto} steps: engine-vs-reference {err:.3e}")
+        assert err <= 1e-12
