@@ -81,7 +81,8 @@ __host__ __device__ inline long long adj_cell(int i, int j, int k, int nx, int n
 // transpose, store lamv[19] of the face (population-major, stride nface).
 template <class T, class S, int AX>
 __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb, const S *__restrict__ lam_next,
-                                                       T *__restrict__ lamv, const StepParams<T, S> P)
+                                                       T *__restrict__ lamv, T *__restrict__ lamF_face,
+                                                       const StepParams<T, S> P)
 {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const long long nface = adj_nface(AX, nx, ny, nz);
@@ -95,6 +96,7 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
         k = int(r / ny) + 1;
         if (P.periodic_x && I == 0) {
             for (int p = 0; p < NPOP; ++p) lamv[p * nface + q] = T(0);  // periodic: face 0 is face nx
+            if (lamF_face) lamF_face[q] = T(0);
             return;
         }
     } else {
@@ -207,21 +209,38 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
     moments(v, r, jx, jy, jz);
     const T inv = T(1) / r;
     const T u0 = jx * inv, v0 = jy * inv, w0 = jz * inv;
+    // face force: ambient plus the field averaged over the two cells
+    T Ff[3] = {P.F[0], P.F[1], P.F[2]};
+    const T fadd = P.ffield ? face_field<T, S, AX>(P, AX == 0 ? I : i, j, k) : T(0);
+    if (P.ffield) Ff[P.ffaxis] += fadd;
+    const T hh = T(0.5) * P.hdt;
     T u = u0, vv = v0, w = w0, B = P.fw2;
-    if (P.force_on) {
-        u += P.hF[0];
-        vv += P.hF[1];
-        w += P.hF[2];
-        B = fma(-P.fw0x3, fma(P.F[0], u, fma(P.F[1], vv, P.F[2] * w)), P.fw2);
+    if (P.force_on || P.ffield) {
+        u = fma(hh, Ff[0], u);
+        vv = fma(hh, Ff[1], vv);
+        w = fma(hh, Ff[2], w);
+        B = fma(-P.fw0x3, fma(Ff[0], u, fma(Ff[1], vv, Ff[2] * w)), P.fw2);
     }
     T fe[NPOP];
     feq_all(r, u, vv, w, fe);
     AdjJac<T> Jc = {T(0), {T(0), T(0), T(0)}};
+    T Sc = T(0), Gq = T(0);  // parts of dJ/dF_face along the field axis
 #pragma unroll
     for (int s = 0; s < 10; ++s) {
         const int p = flux_pop(AX, s);
-        adj_accum(Jc, p, lamF[p], r, u, vv, w, B + P.Kf[p], fe[p], P.fw0x3, P.F);
+        const T cfp = T(cx(p)) * Ff[0] + T(cy(p)) * Ff[1] + T(cz(p)) * Ff[2];
+        const T coef = B + P.fw0x3 * cfp;
+        adj_accum(Jc, p, lamF[p], r, u, vv, w, coef, fe[p], P.fw0x3, Ff);
+        if (P.ffield) {
+            const int ax = P.ffaxis;
+            const T ua = ax == 0 ? u : (ax == 1 ? vv : w);
+            const T ca = T(ax == 0 ? cx(p) : (ax == 1 ? cy(p) : cz(p)));
+            const T cu = T(cx(p)) * u + T(cy(p)) * vv + T(cz(p)) * w;
+            Sc += lamF[p] * (ca - ua - hh * Ff[ax]) * fe[p];
+            Gq += lamF[p] * coef * weight<T>(p) * r * (T(3) * ca + T(9) * cu * ca - T(3) * ua);
+        }
     }
+    if (lamF_face) lamF_face[q] = P.ffield ? P.fw0x3 * Sc + hh * Gq : T(0);
     T lv[NPOP];
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
@@ -335,10 +354,21 @@ __device__ __forceinline__ T adj_received(const T *__restrict__ LX, const T *__r
 }
 
 // mu = 4/3 lam' + (G^T L^T lamv); lam = (dA/df)^T mu - 1/3 lam'.
+// d(face field)/d(phi at column gi) of x face I: (phi(i1) + phi(i2))/2
+template <class T, class S>
+__device__ __forceinline__ T xface_share(const StepParams<T, S> &P, int I, int gi)
+{
+    const int i1 = I == 0 ? (P.periodic_x ? P.nx : 1) : I;
+    const int i2 = I + 1 <= P.nx ? I + 1 : (P.periodic_x ? 1 : P.nx);
+    return T(0.5) * (T(i1 == gi) + T(i2 == gi));
+}
+
 template <class T, class S>
 __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f, const S *__restrict__ lam_next,
                                                          const T *__restrict__ LX, const T *__restrict__ LY,
                                                          const T *__restrict__ LZ, S *__restrict__ lam_out,
+                                                         const T *__restrict__ LFX, const T *__restrict__ LFY,
+                                                         const T *__restrict__ LFZ, double *__restrict__ dphi,
                                                          const StepParams<T, S> P)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -369,7 +399,7 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
     T Fx, Fy, Fz;
     cell_force(P, i - 1, j - 1, k - 1, Fx, Fy, Fz);
     const T Fc[3] = {Fx, Fy, Fz};
-    const bool forced = P.force_on || P.perturb;
+    const bool forced = P.force_on || P.perturb || P.ffield;
     T u = u0, vv = v0, w = w0, B = P.bw2;
     if (forced) {
         u = fma(P.hdt, Fx, u);
@@ -383,7 +413,7 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
         T K = P.Kb[p];
-        if (P.perturb) {
+        if (P.perturb || P.ffield) {
             T cf = T(0);
             if (cx(p)) cf += cx(p) > 0 ? Fx : -Fx;
             if (cy(p)) cf += cy(p) > 0 ? Fy : -Fy;
@@ -397,6 +427,32 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
         const T g = Jc.S0 + Jc.G[0] * (T(cx(p)) - u0) + Jc.G[1] * (T(cy(p)) - v0) + Jc.G[2] * (T(cz(p)) - w0);
         const T out = P.bw1 * mu[p] + g * inv - T(1.0 / 3.0) * T(lam_next[p * P.ps + c]);
         lam_out[p * P.ps + c] = S(out);
+    }
+    if (dphi && P.ffield) {
+        // stage (a): d fb_p / dF_a = 3 bw0 (c_ap - u_a - hdt F_a) feq_p + coef_p hdt d feq_p / d u_a
+        const int ax = P.ffaxis;
+        const T ua = ax == 0 ? u : (ax == 1 ? vv : w);
+        const T Fa = Fc[ax];
+        T Sc = T(0), Gq = T(0);
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) {
+            const T ca = T(ax == 0 ? cx(p) : (ax == 1 ? cy(p) : cz(p)));
+            const T cfp = T(cx(p)) * Fx + T(cy(p)) * Fy + T(cz(p)) * Fz;
+            const T coef = B + P.bw0x3 * cfp;
+            const T cu = T(cx(p)) * u + T(cy(p)) * vv + T(cz(p)) * w;
+            Sc += mu[p] * (ca - ua - P.hdt * Fa) * fe[p];
+            Gq += mu[p] * coef * weight<T>(p) * r * (T(3) * ca + T(9) * cu * ca - T(3) * ua);
+        }
+        double g = double(P.bw0x3 * Sc + P.hdt * Gq);
+        // faces: the field enters each face through the mean over its two cells
+        const int nx = P.nx, ny = P.ny, nz = P.nz;
+        const int Il = P.periodic_x && i == 1 ? nx : i - 1;
+        g += double(xface_share(P, Il, i) * LFX[adj_xface(Il, j, k, nx, ny)]);
+        g += double(xface_share(P, i, i) * LFX[adj_xface(i, j, k, nx, ny)]);
+        const int jl = j == 1 ? ny : j - 1, kl = k == 1 ? nz : k - 1;
+        g += 0.5 * double(LFY[adj_cell(i, jl, k, nx, ny)]) + 0.5 * double(LFY[adj_cell(i, j, k, nx, ny)]);
+        g += 0.5 * double(LFZ[adj_cell(i, j, kl, nx, ny)]) + 0.5 * double(LFZ[adj_cell(i, j, k, nx, ny)]);
+        dphi[adj_cell(i, j, k, nx, ny)] += g;
     }
 }
 

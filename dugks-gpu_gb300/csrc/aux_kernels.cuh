@@ -84,23 +84,25 @@ __global__ void stats_reduce_kernel(const double *__restrict__ partial, int nblo
 __global__ void stats_accumulate_kernel(const double *__restrict__ total, int nx, double *__restrict__ acc);
 
 // Conserved moments: block partial sums of (rho, jx, jy, jz) over cells.
+// Block b owns rows (j,k) = b, b+gridDim.x, ...; threads stride x (coalesced);
+// fixed assignment and a fixed-order tree make the sums reproducible.
 template <class T, class S>
 __global__ void __launch_bounds__(256) moments_partials_kernel(const S *__restrict__ f, const StepParams<T, S> P,
                                                                double *__restrict__ partial)
 {
     __shared__ double red[4][256];
     double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
-    const long long ncell = (long long)P.nx * P.ny * P.nz;
-    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < ncell; q += (long long)gridDim.x * blockDim.x) {
-        const long long row = q / P.nx;
-        const int i = int(q - row * P.nx);
-        const long long c = row * P.pitch + i;
-        double v[NPOP];
+    const int rows = P.ny * P.nz;
+    for (int row = blockIdx.x; row < rows; row += gridDim.x) {
+        for (int i = threadIdx.x; i < P.nx; i += blockDim.x) {
+            const long long c = (long long)row * P.pitch + i;
+            double v[NPOP];
 #pragma unroll
-        for (int p = 0; p < NPOP; ++p) v[p] = double(P.codec.load_nc(f, p * P.ps + c, p));
-        double r, jx, jy, jz;
-        moments(v, r, jx, jy, jz);
-        a0 += r; a1 += jx; a2 += jy; a3 += jz;
+            for (int p = 0; p < NPOP; ++p) v[p] = double(P.codec.load_nc(f, p * P.ps + c, p));
+            double r, jx, jy, jz;
+            moments(v, r, jx, jy, jz);
+            a0 += r; a1 += jx; a2 += jy; a3 += jz;
+        }
     }
     red[0][threadIdx.x] = a0; red[1][threadIdx.x] = a1; red[2][threadIdx.x] = a2; red[3][threadIdx.x] = a3;
     __syncthreads();

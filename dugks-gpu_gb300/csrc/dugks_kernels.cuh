@@ -71,6 +71,10 @@ struct StepParams {
     const T *pert_z;             // [nz+2][3]: cos(gamma zz), sin(gamma zz), 0
     T pert_ax, pert_ay, pert_az, pert_FF;  // per-step amplitude prefactors
     int *err;                    // device error flag (bit 0: a TMA pipeline wait gave up)
+    // optional per-cell body-force field phi (an extension): F(cell) = F_ambient + phi(cell) e_ffaxis in
+    // stage (a), F(face) = F_ambient + (phi(c1) + phi(c2))/2 e_ffaxis on a face between c1 and c2
+    const T *ffield;             // [k][j][pitch] like one population of f-tilde; nullptr = none
+    int ffaxis;
     Codec<T, S> codec;           // storage decode / encode constants
 };
 
@@ -151,6 +155,10 @@ template <class T, class S>
 __device__ __forceinline__ void cell_force(const StepParams<T, S> &P, int i, int j, int k, T &Fx, T &Fy, T &Fz)
 {
     Fx = P.F[0]; Fy = P.F[1]; Fz = P.F[2];
+    if (P.ffield) {
+        const T phi = __ldg(P.ffield + ((long long)k * P.ny + j) * P.pitch + i);
+        if (P.ffaxis == 0) Fx += phi; else if (P.ffaxis == 1) Fy += phi; else Fz += phi;
+    }
     if (P.perturb) {
         // 1-based cell (i+1, j+1, k+1); zone flag set for 3 < i < nx/4 + 2 (src/dugks.cu:1112)
         const T *px = P.pert_x + 3 * (i + 1);
@@ -185,7 +193,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
 
     T Fx, Fy, Fz;
     cell_force(P, i, j, k, Fx, Fy, Fz);
-    const bool forced = P.force_on || P.perturb;
+    const bool forced = P.force_on || P.perturb || P.ffield;
     if (forced) {
         u = fma(P.hdt, Fx, u);
         vv = fma(P.hdt, Fy, vv);
@@ -201,7 +209,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
         T K = P.Kb[p];
-        if (P.perturb) {
+        if (P.perturb || P.ffield) {
             T cf = T(0);
             if (cx(p)) cf += cx(p) > 0 ? Fx : -Fx;
             if (cy(p)) cf += cy(p) > 0 ? Fy : -Fy;
@@ -320,13 +328,16 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
     const int km = k - 1, kp = k + 1, kc = k;
     if (AX == 0) {
         const int A = i == 0 ? 1 : i, B = i == 0 ? 0 : i + 1;
+        // the x weights depend on p only through cx(p): read them at the
+        // representative population (1: cx>0, 2: cx<0, 3: cx=0), one load per class
         const T *xw = P.xw + (size_t)i * 38;
         const RI r00 = R.rb(jc, kc);
         v[0] = T(0.5) * (R(0, r00, A) + R(0, r00, B));
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ay = cy(p), az = cz(p);
-            const T om = __ldg(xw + 2 * p), m = __ldg(xw + 2 * p + 1);
+            const int rp = cx(p) > 0 ? 1 : (cx(p) < 0 ? 2 : 3);
+            const T om = __ldg(xw + 2 * rp), m = __ldg(xw + 2 * rp + 1);
             const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
             const int kt = az > 0 ? km : (az < 0 ? kp : kc);
             const T x00 = lerp2(om, m, R(p, r00, A), R(p, r00, B));
@@ -359,7 +370,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
             const int io = i - ax;
             const int kt = az > 0 ? km : (az < 0 ? kp : kc);
             T txo = T(1), txm = T(0);
-            if (ax) { txo = __ldg(tw + 2 * p); txm = __ldg(tw + 2 * p + 1); }
+            if (ax) { txo = __ldg(tw + (ax > 0 ? 2 : 4)); txm = __ldg(tw + (ax > 0 ? 3 : 5)); }  // rep. 1 / 2
             T x00 = R(p, rA, i), x01 = R(p, rB, i);
             if (ax) {
                 x00 = lerp2(txo, txm, x00, R(p, rA, io));
@@ -389,7 +400,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
             const int io = i - ax;
             const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
             T txo = T(1), txm = T(0);
-            if (ax) { txo = __ldg(tw + 2 * p); txm = __ldg(tw + 2 * p + 1); }
+            if (ax) { txo = __ldg(tw + (ax > 0 ? 2 : 4)); txm = __ldg(tw + (ax > 0 ? 3 : 5)); }  // rep. 1 / 2
             T x00 = R(p, rA, i), x10 = R(p, rB, i);
             if (ax) {
                 x00 = lerp2(txo, txm, x00, R(p, rA, io));
@@ -465,19 +476,28 @@ __device__ __forceinline__ void face_grad(const StepParams<T, S> &P, const RD &R
 // for the 10 populations crossing a face normal to AX.  Stored divided by fw1
 // (out_s = F_p / fw1, one FMA each); the update multiplies the flux
 // differences by fw1 dt/dx instead.
-template <class T, class S, int AX>
-__device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[NPOP], T out[10])
+template <class T, class S, int AX, bool FF>
+__device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[NPOP], T out[10], T fadd)
 {
     T r, jx, jy, jz;
     moments(v, r, jx, jy, jz);
     const T inv = recip(r);
     T u = jx * inv, vv = jy * inv, w = jz * inv;
     T B = P.fw2s;
-    if (P.force_on) {
+    T Ff[3] = {P.F[0], P.F[1], P.F[2]};
+    if (FF) {
+        // face force with the field: shift (hdt/2) F_face
+        Ff[P.ffaxis] += fadd;
+        const T hh = T(0.5) * P.hdt;
+        u = fma(hh, Ff[0], u);
+        vv = fma(hh, Ff[1], vv);
+        w = fma(hh, Ff[2], w);
+        B = fma(-P.fw0x3s, fma(Ff[0], u, fma(Ff[1], vv, Ff[2] * w)), P.fw2s);
+    } else if (P.force_on) {
         u += P.hF[0];
         vv += P.hF[1];
         w += P.hF[2];
-        B = fma(-P.fw0x3s, fma(P.F[0], u, fma(P.F[1], vv, P.F[2] * w)), P.fw2s);
+        B = fma(-P.fw0x3s, fma(Ff[0], u, fma(Ff[1], vv, Ff[2] * w)), P.fw2s);
     }
     const T u3 = T(3) * u, v3 = T(3) * vv, w3 = T(3) * w;
     const T base = fma(T(-1.5), fma(u, u, fma(vv, vv, w * w)), T(1));
@@ -505,8 +525,36 @@ __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[N
 #pragma unroll
     for (int s = 0; s < 10; ++s) {
         const int p = flux_pop(AX, s);
-        out[s] = fma(B + P.Kfs[p], fe[p], v[p]);
+        T K = P.Kfs[p];
+        if (FF) {
+            const int ca = P.ffaxis == 0 ? cx(p) : (P.ffaxis == 1 ? cy(p) : cz(p));
+            if (ca) K = fma(ca > 0 ? P.fw0x3s : -P.fw0x3s, fadd, K);
+        }
+        out[s] = fma(B + K, fe[p], v[p]);
     }
+}
+
+// Force-field contribution on a face: the mean of phi over the two cells
+// across the face (one cell on a wall face).  i, j, k: the face's stored
+// indices as passed to face_fluxes.
+template <class T, class S, int AX>
+__device__ __forceinline__ T face_field(const StepParams<T, S> &P, int i, int j, int k)
+{
+    if (!P.ffield) return T(0);
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    auto wr1 = [](int a, int n) { return a < 1 ? a + n : (a > n ? a - n : a); };
+    int i1 = i, i2 = i, j1 = wr1(j, ny), j2 = j1, k1 = wr1(k, nz), k2 = k1;
+    if (AX == 0) {
+        i1 = i == 0 ? (P.periodic_x ? nx : 1) : i;
+        i2 = i + 1 <= nx ? i + 1 : (P.periodic_x ? 1 : nx);
+    } else if (AX == 1) {
+        j2 = wr1(j + 1, ny);
+    } else {
+        k2 = wr1(k + 1, nz);
+    }
+    const T a = __ldg(P.ffield + ((long long)(k1 - 1) * ny + (j1 - 1)) * P.pitch + (i1 - 1));
+    const T b = __ldg(P.ffield + ((long long)(k2 - 1) * ny + (j2 - 1)) * P.pitch + (i2 - 1));
+    return T(0.5) * (a + b);
 }
 
 // Bounce-back on the wall faces (src/dugks.cu:807-823): the populations
@@ -523,7 +571,7 @@ __device__ __forceinline__ void bounce_back(T v[NPOP], bool lo, bool hi)
 }
 
 // Fluxes of one face: reconstruction + bounce-back + face equilibrium.
-template <class T, class S, int AX, int RECON, class RD>
+template <class T, class S, int AX, int RECON, bool FF, class RD>
 __device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const RD &R, int i, int j, int k, T out[10])
 {
     T v[NPOP];
@@ -532,10 +580,10 @@ __device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const RD 
     else
         face_grad<T, S, AX>(P, R, i, j, k, v);
     if (AX == 0 && !P.periodic_x) bounce_back(v, i == 0, i == P.nx);
-    face_flux<T, S, AX>(P, v, out);
+    face_flux<T, S, AX, FF>(P, v, out, FF ? face_field<T, S, AX>(P, i, j, k) : T(0));
 }
 
-template <class T, class S, int W, int RECON, int MINB>
+template <class T, class S, int W, int RECON, int MINB, bool FF>
 __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict__ fb, const S *f_in, S *f_out,
                                                        const StepParams<T, S> P, int kchunk)
 {
@@ -562,21 +610,21 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict_
     T fzd[10], fzu[10], fx[10], fy[10];
     int buf = 0;
     if (kb >= ke) return;
-    if (wr >= 1) face_fluxes<T, S, 2, RECON>(P, R, ci, cj, kb - 1, fzd);  // z face kb-1/2
+    if (wr >= 1) face_fluxes<T, S, 2, RECON, FF>(P, R, ci, cj, kb - 1, fzd);  // z face kb-1/2
     for (int k = kb; k < ke; ++k) {
         if (wr >= 1) {
-            face_fluxes<T, S, 0, RECON>(P, R, ci, cj, k, fx);   // +x face I = gi
-            face_fluxes<T, S, 1, RECON>(P, R, ci, cj, k, fy);   // +y face J = gj
-            face_fluxes<T, S, 2, RECON>(P, R, ci, cj, k, fzu);  // +z face k+1/2
+            face_fluxes<T, S, 0, RECON, FF>(P, R, ci, cj, k, fx);   // +x face I = gi
+            face_fluxes<T, S, 1, RECON, FF>(P, R, ci, cj, k, fy);   // +y face J = gj
+            face_fluxes<T, S, 2, RECON, FF>(P, R, ci, cj, k, fzu);  // +z face k+1/2
 #pragma unroll
             for (int s = 0; s < 10; ++s) ysh[buf][wr][s][lane] = fy[s];
         } else {
-            face_fluxes<T, S, 1, RECON>(P, R, ci, j0 - 1, k, fy);  // y face J = j0-1 (may be 0: periodic image)
+            face_fluxes<T, S, 1, RECON, FF>(P, R, ci, j0 - 1, k, fy);  // y face J = j0-1 (may be 0: periodic image)
 #pragma unroll
             for (int s = 0; s < 10; ++s) ysh[buf][0][s][lane] = fy[s];
             if (hx) {
                 T hxf[10];
-                face_fluxes<T, S, 0, RECON>(P, R, i0 - 1, hj, k, hxf);  // x face I = i0-1 of row hj
+                face_fluxes<T, S, 0, RECON, FF>(P, R, i0 - 1, hj, k, hxf);  // x face I = i0-1 of row hj
 #pragma unroll
                 for (int s = 0; s < 10; ++s) xsh[buf][lane + 1][s] = hxf[s];
             }
@@ -671,7 +719,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
     return false;
 }
 
-template <class T, class S, int W, int RECON, int MINB>
+template <class T, class S, int W, int RECON, int MINB, bool FF>
 __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_constant__ CUtensorMap tmap,
                                                                  const S *f_in, S *f_out,
                                                                  const StepParams<T, S> P, int kchunk)
@@ -732,22 +780,22 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
     int buf = 0;
     wait(kb - 1);
     wait(kb);
-    if (wr >= 1) face_fluxes<T, S, 2, RECON>(P, R, ci, cj, kb - 1, fzd);
+    if (wr >= 1) face_fluxes<T, S, 2, RECON, FF>(P, R, ci, cj, kb - 1, fzd);
     for (int k = kb; k < ke; ++k) {
         wait(k + 1);
         if (wr >= 1) {
-            face_fluxes<T, S, 0, RECON>(P, R, ci, cj, k, fx);
-            face_fluxes<T, S, 1, RECON>(P, R, ci, cj, k, fy);
-            face_fluxes<T, S, 2, RECON>(P, R, ci, cj, k, fzu);
+            face_fluxes<T, S, 0, RECON, FF>(P, R, ci, cj, k, fx);
+            face_fluxes<T, S, 1, RECON, FF>(P, R, ci, cj, k, fy);
+            face_fluxes<T, S, 2, RECON, FF>(P, R, ci, cj, k, fzu);
 #pragma unroll
             for (int s = 0; s < 10; ++s) ysh[buf][wr][s][lane] = fy[s];
         } else {
-            face_fluxes<T, S, 1, RECON>(P, R, ci, j0 - 1, k, fy);
+            face_fluxes<T, S, 1, RECON, FF>(P, R, ci, j0 - 1, k, fy);
 #pragma unroll
             for (int s = 0; s < 10; ++s) ysh[buf][0][s][lane] = fy[s];
             if (hx) {
                 T hxf[10];
-                face_fluxes<T, S, 0, RECON>(P, R, i0 - 1, hj, k, hxf);
+                face_fluxes<T, S, 0, RECON, FF>(P, R, i0 - 1, hj, k, hxf);
 #pragma unroll
                 for (int s = 0; s < 10; ++s) xsh[buf][lane + 1][s] = hxf[s];
             }

@@ -131,6 +131,9 @@ struct dg_ctx {
     double *scratch = nullptr;    // statistics partial sums / moments partials
     size_t scratch_bytes = 0;
     void *adj = nullptr;          // per-face adjoint scratch (allocated on first dg_adjoint_step)
+    void *ffield = nullptr;       // body-force field phi, T-typed, [k][j][pitch] (dg_set_force_field)
+    int ffaxis = 0;
+    double *dphi = nullptr;       // accumulated dJ/dphi, [k][j][i] (adjoint steps with a field)
     double *acc = nullptr;        // running sums of the per-x statistics (dg_stats_accumulate)
     int *dev_err = nullptr;       // device error flag written by the kernels (TMA wait time-outs)
     CUtensorMap tmap;             // f-bar-plus tensor map of the TMA flux kernel (64-byte aligned type)
@@ -146,6 +149,8 @@ struct dg_ctx {
         if (macro) cudaFree(macro);
         if (scratch) cudaFree(scratch);
         if (adj) cudaFree(adj);
+        if (ffield) cudaFree(ffield);
+        if (dphi) cudaFree(dphi);
         if (acc) cudaFree(acc);
         if (dev_err) cudaFree(dev_err);
     }
@@ -426,6 +431,8 @@ StepParams<T, S> params_for(const dg_ctx *h, int istep)
     else
         P = make_params<T, S>(h, h->c32);
     set_codec<T, S>(h, P.codec);
+    P.ffield = static_cast<const T *>(h->ffield);
+    P.ffaxis = h->ffaxis;
     if (h->perturb) {
         // per-step amplitudes, src/dugks.cu:1101-1108
         const double pi = 3.141592653589793, pi2 = pi * 2;
@@ -580,7 +587,7 @@ template <class T, class S>
 int moments_form(dg_ctx *h, double *out4)
 {
     using K = Kern<T, S>;
-    const int nb = 304;
+    const int nb = 608;
     int rc = ensure_scratch(h, size_t(nb) * 4 * sizeof(double));
     if (rc) return rc;
     CK(K::moments_partials(static_cast<const S *>(h->f), params_for<T, S>(h, 0), h->scratch, nb, h->stream),
@@ -601,11 +608,17 @@ int adjoint_form(dg_ctx *h, int istep, const void *f_n, const void *lam_next, vo
     using K = Kern<T, S>;
     if (!std::is_same<T, S>::value) return h->fail(DG_ERR_UNSUPPORTED, "the adjoint exists for the fp64 and fp32 forms");
     if (!h->adj) {
+        // 19 adjoint values and one dJ/dF (force-field face term) per face
         const long long n = adj_nface(0, h->nx, h->ny, h->nz) + 2 * adj_nface(1, h->nx, h->ny, h->nz);
-        CK(cudaMalloc(&h->adj, size_t(n) * NPOP * sizeof(T)), "cudaMalloc (adjoint scratch)");
+        CK(cudaMalloc(&h->adj, size_t(n) * (NPOP + 1) * sizeof(T)), "cudaMalloc (adjoint scratch)");
+    }
+    if (h->ffield && !h->dphi) {
+        CK(cudaMalloc(&h->dphi, h->ncell() * sizeof(double)), "cudaMalloc (field gradient)");
+        CK(cudaMemsetAsync(h->dphi, 0, h->ncell() * sizeof(double), h->stream), "cudaMemset (field gradient)");
     }
     CK(K::adjoint(static_cast<const S *>(f_n), static_cast<S *>(h->fb), static_cast<const S *>(lam_next),
-                  static_cast<S *>(lam_out), static_cast<T *>(h->adj), params_for<T, S>(h, istep), h->stream),
+                  static_cast<S *>(lam_out), static_cast<T *>(h->adj), params_for<T, S>(h, istep),
+                  h->ffield ? h->dphi : nullptr, h->stream),
        "adjoint launch");
     h->macro_valid = false;
     return DG_OK;
@@ -1250,6 +1263,53 @@ int dg_adjoint_step(dg_t *h, int istep, const void *f_n, const void *lam_next, v
     if (f_n == h->fb || lam_next == h->fb || lam_out == h->fb || f_n == lam_out)
         return h->fail(DG_ERR_ARG, "adjoint buffers must not alias f-bar-plus or each other (lam_out may equal lam_next)");
     return DISPATCH(h, adjoint_form, istep, f_n, lam_next, lam_out);
+}
+
+int dg_set_force_field(dg_t *h, int axis, const double *phi)
+{
+    if (!h) return DG_ERR_ARG;
+    if (!phi) {
+        if (h->ffield) CK(cudaFree(h->ffield), "cudaFree (force field)");
+        h->ffield = nullptr;
+        return DG_OK;
+    }
+    if (axis < 0 || axis > 2) return h->fail(DG_ERR_ARG, "force-field axis must be 0 (x), 1 (y) or 2 (z)");
+    if (h->perturb) return h->fail(DG_ERR_UNSUPPORTED, "a force field cannot be combined with perturb=1");
+    const size_t es = h->prec == DG_PREC_FP64 ? sizeof(double) : sizeof(float);
+    const size_t n = size_t(h->pitch) * h->ny * h->nz;
+    std::vector<char> buf(n * es, 0);
+    for (int k = 0; k < h->nz; ++k)
+        for (int j = 0; j < h->ny; ++j)
+            for (int i = 0; i < h->nx; ++i) {
+                const double v = phi[(size_t(k) * h->ny + j) * h->nx + i];
+                if (!std::isfinite(v)) return h->fail(DG_ERR_NUMERIC, "force field holds a non-finite value");
+                const size_t c = (size_t(k) * h->ny + j) * h->pitch + i;
+                if (es == sizeof(double)) reinterpret_cast<double *>(buf.data())[c] = v;
+                else reinterpret_cast<float *>(buf.data())[c] = float(v);
+            }
+    if (!h->ffield) CK(cudaMalloc(&h->ffield, buf.size()), "cudaMalloc (force field)");
+    // synchronous: the host buffer is released on return and earlier steps may still read the old field
+    CK(cudaStreamSynchronize(h->stream), "force-field sync");
+    CK(cudaMemcpy(h->ffield, buf.data(), buf.size(), cudaMemcpyHostToDevice), "force-field copy");
+    h->ffaxis = axis;
+    return DG_OK;
+}
+
+int dg_field_grad(dg_t *h, double *dphi, int reset)
+{
+    if (!h) return DG_ERR_ARG;
+    if (dphi) {
+        if (h->dphi) {
+            CK(cudaMemcpyAsync(dphi, h->dphi, h->ncell() * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+               "field-gradient copy");
+            CK(cudaStreamSynchronize(h->stream), "field-gradient sync");
+        } else {
+            std::fill(dphi, dphi + h->ncell(), 0.0);
+        }
+    }
+    if (reset && h->dphi)
+        CK(cudaMemsetAsync(h->dphi, 0, h->ncell() * sizeof(double), h->stream), "cudaMemset (field gradient)");
+    return DG_OK;
 }
 
 int dg_get_state_device(dg_t *h, void *dst)

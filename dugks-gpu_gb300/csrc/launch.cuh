@@ -54,8 +54,9 @@ struct Kern {
     // Adjoint of one step (adjoint_kernels.cuh): recomputes f-bar-plus of f_n into fb,
     // per-face adjoints into lamv (T-typed scratch, adj_nface(0)+2*adj_nface(1) faces x 19),
     // then lam_out = (dS/df)^T lam_next.  FP64 and FP32 forms only.
+    // dphi (optional, FP64, dump order [k][j][i]): += dJ/dphi of this step when a force field is set
     static cudaError_t adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_out, T *lamv,
-                               const StepParams<T, S> &P, cudaStream_t st);
+                               const StepParams<T, S> &P, double *dphi, cudaStream_t st);
     static int flux_kchunk(const StepParams<T, S> &P);
 };
 

@@ -26,11 +26,11 @@ int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int occ = 1;
-    if (TileCfg<T, S>::TMA)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_tma_kernel<T, S, W, 0, MB>, 32 * W,
+    if constexpr (TileCfg<T, S>::TMA)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_tma_kernel<T, S, W, 0, MB, false>, 32 * W,
                                                       flux_tma_smem_bytes<T, S, W>());
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0, MB>, 32 * W, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0, MB, false>, 32 * W, 0);
     occ = std::max(occ, 1);
     const long long cols = (long long)((P.nx + 31) / 32) * ((P.ny + W - 2) / (W - 1));
     const long long want = 4LL * sms * occ;
@@ -41,39 +41,43 @@ int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
     return int((P.nz + nchunks - 1) / nchunks);
 }
 
+// one launch of the flux kernel variant <RECON, FF>
+template <class T, class S, int RECON, bool FF>
+static cudaError_t flux_launch(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P,
+                               const CUtensorMap *tmap, int kchunk, cudaStream_t st)
+{
+    constexpr int W = TileCfg<T, S>::W, MB = TileCfg<T, S>::MINB;
+    dim3 grid((P.nx + 31) / 32, (P.ny + W - 2) / (W - 1), (P.nz + kchunk - 1) / kchunk);
+    dim3 block(32, W);
+    if constexpr (TileCfg<T, S>::TMA) {
+        auto kern = flux_tma_kernel<T, S, W, RECON, MB, FF>;
+        const int bytes = int(flux_tma_smem_bytes<T, S, W>());
+        static bool attr_set = false;
+        if (!attr_set) {
+            const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+            if (e != cudaSuccess) return e;
+            attr_set = true;
+        }
+        if (!tmap) return cudaErrorInvalidValue;
+        kern<<<grid, block, bytes, st>>>(*tmap, f_in, f_out, P, kchunk);
+    } else {
+        (void)tmap;
+        flux_kernel<T, S, W, RECON, MB, FF><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
+    }
+    return cudaGetLastError();
+}
+
 template <class T, class S>
 cudaError_t Kern<T, S>::flux(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P, int recon,
                              const CUtensorMap *tmap, cudaStream_t st)
 {
-    constexpr int W = TileCfg<T, S>::W, MB = TileCfg<T, S>::MINB;
-    static bool attr_set = false;
-    if (TileCfg<T, S>::TMA && !attr_set) {
-        const int bytes = int(flux_tma_smem_bytes<T, S, W>());
-        cudaError_t e = cudaFuncSetAttribute(flux_tma_kernel<T, S, W, 0, MB>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(flux_tma_kernel<T, S, W, 1, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     bytes);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
     const int kchunk = flux_kchunk(P);
-    dim3 grid((P.nx + 31) / 32, (P.ny + W - 2) / (W - 1), (P.nz + kchunk - 1) / kchunk);
-    dim3 block(32, W);
-    if (TileCfg<T, S>::TMA) {
-        if (!tmap) return cudaErrorInvalidValue;
-        const size_t bytes = flux_tma_smem_bytes<T, S, W>();
-        if (recon == 1)
-            flux_tma_kernel<T, S, W, 1, MB><<<grid, block, bytes, st>>>(*tmap, f_in, f_out, P, kchunk);
-        else
-            flux_tma_kernel<T, S, W, 0, MB><<<grid, block, bytes, st>>>(*tmap, f_in, f_out, P, kchunk);
-        return cudaGetLastError();
-    }
+    const bool ff = P.ffield != nullptr;
     if (recon == 1)
-        flux_kernel<T, S, W, 1, MB><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
-    else
-        flux_kernel<T, S, W, 0, MB><<<grid, block, 0, st>>>(fb, f_in, f_out, P, kchunk);
-    return cudaGetLastError();
+        return ff ? flux_launch<T, S, 1, true>(fb, f_in, f_out, P, tmap, kchunk, st)
+                  : flux_launch<T, S, 1, false>(fb, f_in, f_out, P, tmap, kchunk, st);
+    return ff ? flux_launch<T, S, 0, true>(fb, f_in, f_out, P, tmap, kchunk, st)
+              : flux_launch<T, S, 0, false>(fb, f_in, f_out, P, tmap, kchunk, st);
 }
 
 template <class T, class S>
@@ -124,7 +128,7 @@ cudaError_t Kern<T, S>::moments_partials(const S *f, const StepParams<T, S> &P, 
 
 template <class T, class S>
 cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_out, T *lamv,
-                                const StepParams<T, S> &P, cudaStream_t st)
+                                const StepParams<T, S> &P, double *dphi, cudaStream_t st)
 {
     if constexpr (!std::is_same<T, S>::value) {
         return cudaErrorNotSupported;
@@ -133,13 +137,14 @@ cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_o
         if (e != cudaSuccess) return e;
         const long long nfx = adj_nface(0, P.nx, P.ny, P.nz), nfc = adj_nface(1, P.nx, P.ny, P.nz);
         T *LX = lamv, *LY = lamv + NPOP * nfx, *LZ = LY + NPOP * nfc;
-        adj_face_kernel<T, S, 0><<<unsigned((nfx + 127) / 128), 128, 0, st>>>(fb, lam_next, LX, P);
-        adj_face_kernel<T, S, 1><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LY, P);
-        adj_face_kernel<T, S, 2><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LZ, P);
+        T *LFX = LZ + NPOP * nfc, *LFY = LFX + nfx, *LFZ = LFY + nfc;  // per-face dJ/dF (force field)
+        adj_face_kernel<T, S, 0><<<unsigned((nfx + 127) / 128), 128, 0, st>>>(fb, lam_next, LX, LFX, P);
+        adj_face_kernel<T, S, 1><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LY, LFY, P);
+        adj_face_kernel<T, S, 2><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LZ, LFZ, P);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         dim3 grid((P.nx + 127) / 128, P.ny, P.nz);
-        adj_gather_kernel<T, S><<<grid, 128, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, P);
+        adj_gather_kernel<T, S><<<grid, 128, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, LFX, LFY, LFZ, dphi, P);
         return cudaGetLastError();
     }
 }

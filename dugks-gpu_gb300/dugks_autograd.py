@@ -15,6 +15,7 @@ engine's kernels.
 import torch
 
 import pydugks
+import revolve
 
 _TORCH_DTYPE = {0: torch.float64, 1: torch.float32}
 
@@ -94,6 +95,178 @@ class DugksRun(torch.autograd.Function):
 
 def run(f0, eng, istep0, nsteps, every=100):
     return DugksRun.apply(f0, eng, istep0, nsteps, every)
+
+
+class DugksObjectiveRun(torch.autograd.Function):
+    """(f0, phi) -> (f_n, J), J = (1/n) sum_{k=1..n} objective(f_k, phi).
+
+    phi (nz, ny, nx) is the engine's body-force field along `axis`
+    (dg_set_force_field).  The backward reverses the n steps with the binomial
+    checkpointing schedule of revolve.py using `snaps` stored states besides
+    f0; the state-side gradient runs the hand-written adjoint kernels
+    (dg_adjoint_step), which also accumulate dJ/dphi of every step
+    (dg_field_grad).  The objective's own gradients (the source added to the
+    adjoint at each state and its direct dependence on phi) come from torch
+    autograd on `objective`, or from `objective.accumulate(lam, state, phi,
+    weight)` when the objective provides it (returns d/dphi of weight * g).
+    """
+
+    @staticmethod
+    def forward(ctx, f0, phi, eng, istep0, nsteps, snaps, objective, axis):
+        _sync_stream(eng)
+        eng.set_force_field(axis, phi.detach().double().cpu().numpy())
+        acts = revolve.actions(nsteps, snaps)
+        end, last = revolve.spine(acts)
+        stored = {0: f0.detach().clone()}
+        eng.set_state_device(f0.data_ptr())
+        cur = empty_state(eng, f0.device)
+        J = torch.zeros((), dtype=torch.float64, device=f0.device)
+        phi_d = phi.detach()
+
+        def advance(a, b):
+            for k in range(a, b):
+                eng.step(istep0 + k)
+                eng.get_state_device(cur.data_ptr())
+                with torch.no_grad():
+                    J.add_(objective(cur, phi_d).double())
+
+        k = 0
+        for a in acts[:end]:
+            if a[0] == "advance":
+                advance(a[1], a[2])
+                k = a[2]
+            else:
+                st = empty_state(eng, f0.device)
+                eng.get_state_device(st.data_ptr())
+                stored[a[1]] = st
+        advance(k, nsteps)
+        out = empty_state(eng, f0.device)
+        eng.get_state_device(out.data_ptr())
+        ctx.eng, ctx.istep0, ctx.nsteps, ctx.objective, ctx.axis = eng, istep0, nsteps, objective, axis
+        ctx.acts, ctx.end, ctx.last, ctx.stored = acts, end, last, stored
+        ctx.save_for_backward(phi)
+        return out, J / nsteps
+
+    @staticmethod
+    def backward(ctx, lam_out, gJ):
+        eng, istep0, n, objective = ctx.eng, ctx.istep0, ctx.nsteps, ctx.objective
+        (phi,) = ctx.saved_tensors
+        _sync_stream(eng)
+        dev = lam_out.device if lam_out is not None else phi.device
+        w = (gJ.double() / n) if gJ is not None else torch.zeros((), dtype=torch.float64, device=dev)
+        eng.set_force_field(ctx.axis, phi.detach().double().cpu().numpy())
+        eng.field_grad(reset=True)
+        stored = ctx.stored
+        if lam_out is None:
+            lam = torch.zeros_like(stored[0])
+        else:
+            lam = lam_out.detach().contiguous().clone()
+        dphi_direct = torch.zeros(phi.shape, dtype=torch.float64, device=phi.device)
+        cur = empty_state(eng, lam.device)
+
+        def source(state):
+            nonlocal dphi_direct
+            acc = getattr(objective, "accumulate", None)
+            if acc is not None:
+                dphi_direct += acc(lam, state, phi.detach(), w).double()
+                return
+            with torch.enable_grad():
+                s = state.detach().requires_grad_(True)
+                p = phi.detach().requires_grad_(True)
+                g = objective(s, p).double() * w
+                gs, gp = torch.autograd.grad(g, [s, p], allow_unused=True)
+            if gs is not None:
+                lam.add_(gs.to(lam.dtype))
+            if gp is not None:
+                dphi_direct += gp.double()
+
+        # source at the final state f_n
+        eng.set_state_device(stored[ctx.last].data_ptr())
+        eng.run(istep0 + ctx.last, n - ctx.last) if n > ctx.last else None
+        eng.get_state_device(cur.data_ptr())
+        source(cur)
+        # resume the schedule from the last state of the forward sweep
+        eng.set_state_device(stored[ctx.last].data_ptr())
+        for a in ctx.acts[ctx.end:]:
+            kind = a[0]
+            if kind == "advance":
+                eng.run(istep0 + a[1], a[2] - a[1])
+            elif kind == "store":
+                st = empty_state(eng, lam.device)
+                eng.get_state_device(st.data_ptr())
+                stored[a[1]] = st
+            elif kind == "restore":
+                eng.set_state_device(stored[a[1]].data_ptr())
+            elif kind == "release":
+                stored.pop(a[1], None)
+            else:  # adjoint of step k at the current state k
+                k = a[1]
+                eng.get_state_device(cur.data_ptr())
+                eng.adjoint_step(istep0 + k, cur.data_ptr(), lam.data_ptr(), lam.data_ptr())
+                if k >= 1:
+                    source(cur)
+        dphi = torch.from_numpy(eng.field_grad(reset=True)).to(phi.device) + dphi_direct
+        ctx.stored = None
+        return lam, dphi.to(phi.dtype), None, None, None, None, None, None
+
+
+def run_objective(f0, phi, eng, istep0, nsteps, objective, snaps=64, axis=2):
+    """f_n, J = DugksObjectiveRun (see its docstring)."""
+    return DugksObjectiveRun.apply(f0, phi, eng, istep0, nsteps, snaps, objective, axis)
+
+
+class WallShear:
+    """Mean wall shear stress of a channel with walls on the two x faces.
+
+    tau = rho nu u_s / d at the first cell of each wall (no-slip wall, d the
+    distance of the cell centre from the wall), u_s the velocity along
+    `axis` including the half-step force shift hdt*F that the reference's
+    output velocity carries, F = ambient + phi; averaged over both walls.
+    With rho u_s = j_s + hdt rho F_s the objective is linear in the state
+    for fixed phi; `accumulate` adds its gradient to the wall planes of the
+    adjoint directly.
+    """
+
+    def __init__(self, eng, axis=2):
+        self.eng, self.axis = eng, axis
+        info = eng.info
+        xc, _ = eng.mesh()
+        xw = eng.info.xwidth
+        self.d0, self.d1 = float(xc[1]), float(xw - xc[eng.nx])
+        self.nu = float(info.visc)
+        self.hdt = 0.5 * float(info.dt)
+        self.F = float(info.ambient[axis])
+        self.area = 2.0 * eng.ny * eng.nz
+        c, _ = lattice(torch.float64, "cpu")
+        self.cs = c[axis]
+
+    def _planes(self, t):
+        v = soa_view(self.eng, t)
+        return v[..., 0], v[..., self.eng.nx - 1]   # (19, nz, ny) each
+
+    def __call__(self, state, phi):
+        lo, hi = self._planes(state)
+        cs = self.cs.to(state.dtype).to(state.device).view(19, 1, 1)
+        tot = 0.0
+        for pl, d, ii in ((lo, self.d0, 0), (hi, self.d1, self.eng.nx - 1)):
+            rho = pl.sum(0)
+            js = (cs * pl).sum(0)
+            Fs = self.F + phi[:, :, ii].to(state.dtype)
+            tot = tot + (self.nu / d) * (js + self.hdt * rho * Fs).sum()
+        return tot / self.area
+
+    def accumulate(self, lam, state, phi, w):
+        lo_l, hi_l = self._planes(lam)
+        lo_s, hi_s = self._planes(state)
+        cs = self.cs.to(lam.dtype).to(lam.device).view(19, 1, 1)
+        dphi = torch.zeros(phi.shape, dtype=torch.float64, device=phi.device)
+        for pl, pst, d, ii in ((lo_l, lo_s, self.d0, 0), (hi_l, hi_s, self.d1, self.eng.nx - 1)):
+            k = w * (self.nu / d) / self.area
+            Fs = (self.F + phi[:, :, ii].double())
+            # d/df_p (j_s + hdt rho F_s) = c_sp + hdt F_s
+            pl.add_((k * (cs.double() + self.hdt * Fs.unsqueeze(0))).to(lam.dtype))
+            dphi[:, :, ii] += k * self.hdt * pst.double().sum(0)
+        return dphi
 
 
 # --- D3Q19 helpers for objectives and controls (torch, differentiable) ---

@@ -107,6 +107,8 @@ def lib():
         "dg_get_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
         "dg_set_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
         "dg_adjoint_step": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+        "dg_set_force_field": (ctypes.c_int, [H, ctypes.c_int, _D]),
+        "dg_field_grad": (ctypes.c_int, [H, _D, ctypes.c_int]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -325,3 +327,19 @@ class Engine:
 
     def device_ptr(self, which):
         return lib().dg_device_ptr(self._h, which)
+
+    # body-force field (extension): phi (nz, ny, nx) along `axis`; None removes it
+    def set_force_field(self, axis, phi):
+        if phi is None:
+            self._check(lib().dg_set_force_field(self._h, 0, None))
+            return
+        a = np.ascontiguousarray(phi, dtype=np.float64)
+        if a.shape != (self.nz, self.ny, self.nx):
+            raise ValueError(f"force field shape {a.shape}, expected {(self.nz, self.ny, self.nx)}")
+        self._check(lib().dg_set_force_field(self._h, int(axis), _ptr(a)))
+
+    def field_grad(self, reset=False):
+        """dJ/dphi accumulated by adjoint_step, shape (nz, ny, nx)."""
+        out = np.empty((self.nz, self.ny, self.nx), dtype=np.float64)
+        self._check(lib().dg_field_grad(self._h, _ptr(out), 1 if reset else 0))
+        return out

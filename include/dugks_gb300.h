@@ -177,6 +177,20 @@ int dg_set_state_device(dg_t *h, const void *src);
  * f_n; lam_out may equal lam_next.  Asynchronous on the handle's stream. */
 int dg_adjoint_step(dg_t *h, int istep, const void *f_n, const void *lam_next, void *lam_out);
 
+/* Body-force field (no counterpart in the reference; the control variable
+ * of the adjoint drag-reduction harness): F(cell) = ambient + phi(cell) e_axis
+ * in stage (a), and on a face the mean of phi over its two cells (the one
+ * interior cell on a wall face).  phi: host array of nx*ny*nz doubles in dump
+ * order (i fastest); NULL removes the field.  Not combinable with perturb=1.
+ * Synchronises the handle's stream. */
+int dg_set_force_field(dg_t *h, int axis, const double *phi);
+
+/* dJ/dphi accumulated by dg_adjoint_step over the steps run while a field was
+ * set (no counterpart in the reference).  dphi: host array of nx*ny*nz
+ * doubles, dump order, may be NULL; reset != 0 zeroes the accumulator after
+ * the copy. */
+int dg_field_grad(dg_t *h, double *dphi, int reset);
+
 /* Cell centres and widths along x, nx+2 entries each (index 0 and nx+1 are
  * the mirrored ghosts of src/fortran/channel/src/dugks.cuf:118-121); either
  * pointer may be NULL. */
