@@ -304,7 +304,7 @@ def main():
     e2e_s = time.perf_counter() - t0
     e2e = {"value": n * K / e2e_s / 1e6, "unit": "MLUPS",
            "h2d_bytes_per_step": state_bytes / K,
-           "d2h_bytes_per_step": state_bytes / K + 304 * 4 * 8,
+           "d2h_bytes_per_step": state_bytes / K + 608 * 4 * 8,
            "what": "dg_set_state(pinned host) + K x (dg_step + dg_moments host read) + dg_get_state(pinned host)"}
     eng.close()
 
