@@ -126,6 +126,28 @@ def ncu_traffic(precision):
         return None
 
 
+def fp64_inst_per_cell(kernel):
+    """FP64 thread instructions per cell of `kernel` from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        return json.load(open(p))["fp64_inst_per_cell"][kernel]
+    except Exception:
+        return None
+
+
+def fp64_pipe_peak(stream):
+    """FP64 FMA thread instructions per second, measured now (dugks-gpu_gb300/libdg_peak.so)."""
+    import ctypes
+    L = ctypes.CDLL(os.path.join(ROOT, "dugks-gpu_gb300", "libdg_peak.so"))
+    L.dg_probe_fp64_fma_rate.restype = ctypes.c_int
+    L.dg_probe_fp64_fma_rate.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+    rate = ctypes.c_double(0.0)
+    rc = L.dg_probe_fp64_fma_rate(ctypes.c_void_p(stream), 20, ctypes.byref(rate))
+    if rc != 0:
+        raise RuntimeError(f"FP64 probe failed with CUDA error {rc}")
+    return rate.value
+
+
 def combine_ranks(world, n_cells, steps, ms_local, dist=None, device="cpu"):
     """Whole-job MLUPS of `world` replicas: every rank advanced n_cells for
     `steps` steps; the job time is the maximum over ranks."""
@@ -318,6 +340,17 @@ def main():
             "kernel_ms": {"fbar_kernel": ms_a / K, "flux_kernel": ms_b / K},
             "step_alg_bytes_per_cell": 95 * info_bytes,
             "step_frac": 95 * info_bytes * n * K / (ms / 1e3) / 1e9 / peak}
+    if args.precision == "fp64":
+        # the FP64 step is bound by FP64 instruction issue: its compute roofline
+        per_cell = fp64_inst_per_cell("flux_kernel")
+        dp_peak = fp64_pipe_peak(torch.cuda.current_stream().cuda_stream)
+        comp = {"bound": "fp64 pipe", "kernel": "flux_kernel", "unit": "T FP64 inst/s", "peak": dp_peak / 1e12,
+                "peak_source": "measured in this run: FP64 FMA chains on every SM (libdg_peak.so)",
+                "fp64_inst_per_cell": per_cell}
+        if per_cell:
+            comp["achieved"] = per_cell * n / (ms_b / K / 1e3) / 1e12
+            comp["frac"] = comp["achieved"] / comp["peak"]
+        roof["compute"] = comp
 
     extras = {}
     if rank == 0 and world == 1 and not args.no_extras:
@@ -345,7 +378,7 @@ def main():
                            "re_tau": 180, "nu": meta["nu"], "alpha": meta["alpha"], "parallelism": f"replicas x{world}",
                            "l2": "inputs larger than L2 (f and f-bar-plus resident, %d MB each)" % (n * 19 * info_bytes // 2**20),
                            "structure": "two-pass (stage a kernel, flux+update kernel)"},
-                "e2e": e2e, "gpu_launches": 2 * K, "roofline": roof, "clocks": clocks}
+                "e2e": e2e, "gpu_launches": 3 * K, "roofline": roof, "clocks": clocks}
         line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:

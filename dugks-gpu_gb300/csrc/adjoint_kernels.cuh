@@ -126,7 +126,8 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
             continue;
         }
         if (AX == 0) {
-            const T om = __ldg(xwf + 2 * p), m = __ldg(xwf + 2 * p + 1);
+            const int rp = xrep(p);
+            const T om = __ldg(xwf + 2 * rp), m = __ldg(xwf + 2 * rp + 1);
             auto xl = [&](int jj, int kk) { return lerp2(om, m, fb_at(fb, P, p, A, jj, kk), fb_at(fb, P, p, Bc, jj, kk)); };
             const T x00 = xl(j, k);
             T y00 = x00;
@@ -142,8 +143,8 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
         } else {
             T txo = T(1), txm = T(0);
             if (ax) {
-                txo = __ldg(P.txw + (size_t)i * 38 + 2 * p);
-                txm = __ldg(P.txw + (size_t)i * 38 + 2 * p + 1);
+                txo = __ldg(P.txw + (size_t)i * 38 + 2 * xrep(p));
+                txm = __ldg(P.txw + (size_t)i * 38 + 2 * xrep(p) + 1);
             }
             auto xt = [&](int jj, int kk) {
                 T a = fb_at(fb, P, p, i, jj, kk);
@@ -260,97 +261,182 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
     for (int p = 0; p < NPOP; ++p) lamv[p * nface + q] = lv[p];
 }
 
-// Adjoint received by the f-bar-plus value of population p at column gi
-// (0..nx+1, ghosts included) of row j, plane k, through the interpolation of
-// every face whose stencil contains it (the transpose of L).
-template <class T, class S>
-__device__ __forceinline__ T adj_received(const T *__restrict__ LX, const T *__restrict__ LY,
-                                          const T *__restrict__ LZ, const StepParams<T, S> &P, int p, int gi,
-                                          int j, int k)
-{
-    const int nx = P.nx, ny = P.ny, nz = P.nz;
-    const int ax = cx(p), ay = cy(p), az = cz(p);
-    const long long nfx = adj_nface(0, nx, ny, nz), nfc = adj_nface(1, nx, ny, nz);
-    auto wrapj = [&](int jj) { return jj < 1 ? jj + ny : (jj > ny ? jj - ny : jj); };
-    auto wrapk = [&](int kk) { return kk < 1 ? kk + nz : (kk > nz ? kk - nz : kk); };
-    auto wrapi = [&](int ii) { return ii < 1 ? ii + nx : (ii > nx ? ii - nx : ii); };
-    T acc = T(0);
-    // transverse weights (1-t at the face's own row/plane, t at the shifted one)
-    const T tyo = p == 0 ? T(1) : P.ty_om, tym = P.ty_m, tzo = p == 0 ? T(1) : P.tz_om, tzm = P.tz_m;
+// Row / plane offsets of the face arrays around one interior cell (the
+// periodic images in y and z folded in): x faces ((k-1)*ny + (j-1))*(nx+1),
+// y / z faces ((k-1)*ny + (j-1))*nx, for j-1..j+1 and k-1..k+1.
+struct AdjRows {
+    int x[3][3], c[3][3];  // [dk+1][dj+1]
+};
 
-    // ---- x faces: anchor / other columns ----
-    {
-        auto xsum = [&](int I, T wx) {
-            // rows j' with j = j' (1-ty) or j = j'+cy (ty); planes likewise
-            T s = T(0);
-            const T *base = LX + (long long)p * nfx;
-            s += (ay ? tyo : T(1)) * (az ? tzo : T(1)) * base[adj_xface(I, j, k, nx, ny)];
-            if (ay) s += tym * (az ? tzo : T(1)) * base[adj_xface(I, wrapj(j + ay), k, nx, ny)];
-            if (az) s += (ay ? tyo : T(1)) * tzm * base[adj_xface(I, j, wrapk(k + az), nx, ny)];
-            if (ay && az) s += tym * tzm * base[adj_xface(I, wrapj(j + ay), wrapk(k + az), nx, ny)];
-            return wx * s;
-        };
-        auto xw = [&](int I, int which) -> T {
-            if (p == 0) return T(0.5);
-            return __ldg(P.xw + (size_t)I * 38 + 2 * p + which);
-        };
-        if (P.periodic_x) {
-            // faces I = 1..nx, anchor I, other I+1 (nx+1 -> 1)
-            if (gi >= 1 && gi <= nx) {
-                acc += xsum(gi, xw(gi, 0));
-                const int Io = gi == 1 ? nx : gi - 1;
-                acc += xsum(Io, xw(Io, 1));
-            }
-        } else {
-            if (gi >= 1 && gi <= nx) acc += xsum(gi, xw(gi, 0));      // anchor of face gi
-            if (gi == 1) acc += xsum(0, xw(0, 0));                    // anchor of face 0
-            if (gi >= 2 && gi <= nx + 1) acc += xsum(gi - 1, xw(gi - 1, 1));  // other of face gi-1
-            if (gi == 0) acc += xsum(0, xw(0, 1));                    // other of face 0
+__device__ __forceinline__ AdjRows adj_rows(int j, int k, int nx, int ny, int nz)
+{
+    AdjRows R;
+    const int js[3] = {j == 1 ? ny : j - 1, j, j == ny ? 1 : j + 1};
+    const int ks[3] = {k == 1 ? nz : k - 1, k, k == nz ? 1 : k + 1};
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            const int row = (ks[a] - 1) * ny + (js[b] - 1);
+            R.x[a][b] = row * (nx + 1);
+            R.c[a][b] = row * nx;
         }
+    return R;
+}
+
+// Transposed-stencil sums of one population p (a compile-time constant)
+// around row j, plane k: the adjoint that an f-bar-plus value at column gi
+// receives from the x faces I (xsum) and from the y and z faces at column i
+// (colsum), with the stencil offsets resolved at compile time.
+template <int p, class T, class S>
+struct AdjPop {
+    const T *__restrict__ LX;
+    const T *__restrict__ LY;
+    const T *__restrict__ LZ;
+    const StepParams<T, S> &P;
+    const AdjRows &R;
+    long long nfx, nfc;
+    static constexpr int ax = cx(p), ay = cy(p), az = cz(p), rp = xrep(p);
+
+    __device__ __forceinline__ T xsum(int I) const
+    {
+        const T tyo = p == 0 ? T(1) : P.ty_om, tym = P.ty_m, tzo = p == 0 ? T(1) : P.tz_om, tzm = P.tz_m;
+        const T *base = LX + (long long)p * nfx;
+        T s = (ay ? tyo : T(1)) * (az ? tzo : T(1)) * base[R.x[1][1] + I];
+        if (ay) s += tym * (az ? tzo : T(1)) * base[R.x[1][1 + ay] + I];
+        if (az) s += (ay ? tyo : T(1)) * tzm * base[R.x[1 + az][1] + I];
+        if (ay && az) s += tym * tzm * base[R.x[1 + az][1 + ay] + I];
+        return s;
     }
-    // ---- y and z faces: column i with weight (1-tx(i)) if i = gi, tx(i) if i - cx = gi ----
-    auto colw = [&](int i, int self) -> T {
-        if (!ax) return self ? T(1) : T(0);
-        return __ldg(P.txw + (size_t)i * 38 + 2 * p + (self ? 0 : 1));
-    };
-    int cols[2];
-    T cw[2];
-    int nc = 0;
-    if (gi >= 1 && gi <= nx) { cols[nc] = gi; cw[nc] = colw(gi, 1); ++nc; }
-    if (ax) {
-        int i2 = gi + ax;
-        if (P.periodic_x) i2 = wrapi(i2);
-        if (i2 >= 1 && i2 <= nx && !(P.periodic_x && (gi < 1 || gi > nx))) { cols[nc] = i2; cw[nc] = colw(i2, 0); ++nc; }
+    // x weight of face I: anchor (which = 0) or other column (which = 1)
+    __device__ __forceinline__ T xw(int I, int which) const
+    {
+        return p == 0 ? T(0.5) : __ldg(P.xw + (size_t)I * 38 + 2 * rp + which);
     }
-    for (int c = 0; c < nc; ++c) {
-        const int i = cols[c];
-        const T wc = cw[c];
-        // y faces J (anchor row J = j, other row J+1 = j -> J = j-1)
+    // transverse x weight of the y / z faces at column i: own column (0) or column i - cx (1)
+    __device__ __forceinline__ T tw(int i, int which) const { return __ldg(P.txw + (size_t)i * 38 + 2 * rp + which); }
+    __device__ __forceinline__ T colsum(int i) const
+    {
+        const T tyo = p == 0 ? T(1) : P.ty_om, tym = P.ty_m, tzo = p == 0 ? T(1) : P.tz_om, tzm = P.tz_m;
+        const int c = i - 1;
+        T sy, sz;
         {
             const T *base = LY + (long long)p * nfc;
             const T yo = p == 0 ? T(0.5) : P.yn_om[p], ym = p == 0 ? T(0.5) : P.yn_m[p];
-            T s = yo * base[adj_cell(i, j, k, nx, ny)] + ym * base[adj_cell(i, wrapj(j - 1), k, nx, ny)];
+            sy = yo * base[R.c[1][1] + c] + ym * base[R.c[1][0] + c];
             if (az) {
-                s = (p == 0 ? T(1) : tzo) * s;
-                s += tzm * (yo * base[adj_cell(i, j, wrapk(k + az), nx, ny)] +
-                            ym * base[adj_cell(i, wrapj(j - 1), wrapk(k + az), nx, ny)]);
+                sy = tzo * sy;
+                sy += tzm * (yo * base[R.c[1 + az][1] + c] + ym * base[R.c[1 + az][0] + c]);
             }
-            acc += wc * s;
         }
-        // z faces K (anchor plane K = k, other plane K+1 = k -> K = k-1)
         {
             const T *base = LZ + (long long)p * nfc;
             const T zo = p == 0 ? T(0.5) : P.zn_om[p], zm = p == 0 ? T(0.5) : P.zn_m[p];
-            T s = zo * base[adj_cell(i, j, k, nx, ny)] + zm * base[adj_cell(i, j, wrapk(k - 1), nx, ny)];
+            sz = zo * base[R.c[1][1] + c] + zm * base[R.c[0][1] + c];
             if (ay) {
-                s = tyo * s;
-                s += tym * (zo * base[adj_cell(i, wrapj(j + ay), k, nx, ny)] +
-                            zm * base[adj_cell(i, wrapj(j + ay), wrapk(k - 1), nx, ny)]);
+                sz = tyo * sz;
+                sz += tym * (zo * base[R.c[1][1 + ay] + c] + zm * base[R.c[0][1 + ay] + c]);
             }
-            acc += wc * s;
         }
+        return sy + sz;
     }
-    return acc;
+    // interior column gi (1..nx); Ix2 / x2_anchor: the second x face holding the
+    // column (face gi-1 as "other", face 0 as anchor for gi = 1 between walls,
+    // face nx as "other" for gi = 1 when periodic); i2: the column i with
+    // i - cx = gi of the y / z faces, 0 if none
+    __device__ __forceinline__ T interior(int gi, int Ix2, bool x2_anchor, int i2) const
+    {
+        T acc = xw(gi, 0) * xsum(gi) + xw(Ix2, x2_anchor ? 0 : 1) * xsum(Ix2);
+        if (ax) {
+            acc += tw(gi, 0) * colsum(gi);
+            if (i2 >= 1) acc += tw(i2, 1) * colsum(i2);
+        } else {
+            acc += colsum(gi);
+        }
+        return acc;
+    }
+    // wall ghost column 0 (side 0) or nx+1 (side 1): the other column of x face
+    // 0 / nx, and the y / z faces at column 1 (cx > 0) / nx (cx < 0)
+    __device__ __forceinline__ T ghost(int side) const
+    {
+        const int nx = P.nx;
+        const int I = side ? nx : 0;
+        T acc = xw(I, 1) * xsum(I);
+        if (!side && ax > 0) acc += tw(1, 1) * colsum(1);
+        if (side && ax < 0) acc += tw(nx, 1) * colsum(nx);
+        return acc;
+    }
+};
+
+// Adjoint received by the wall ghost columns (0 and nx+1) of f-bar-plus, per
+// population, row and plane: GH[(side*19 + p) * ny*nz + (k-1)*ny + (j-1)].
+// The gather folds it into columns 1, 2 and nx-1, nx with the extrapolation
+// weights.
+template <class T, class S, int p = 0>
+__device__ __forceinline__ void adj_ghost_pops(const T *LX, const T *LY, const T *LZ, const StepParams<T, S> &P,
+                                               const AdjRows &R, long long nfx, long long nfc, int side,
+                                               T *__restrict__ GH, long long o)
+{
+    const AdjPop<p, T, S> A{LX, LY, LZ, P, R, nfx, nfc};
+    GH[(long long)(side * NPOP + p) * P.ny * P.nz + o] = A.ghost(side);
+    if constexpr (p + 1 < NPOP) adj_ghost_pops<T, S, p + 1>(LX, LY, LZ, P, R, nfx, nfc, side, GH, o);
+}
+
+template <class T, class S>
+__global__ void __launch_bounds__(128) adj_ghost_kernel(const T *__restrict__ LX, const T *__restrict__ LY,
+                                                        const T *__restrict__ LZ, T *__restrict__ GH,
+                                                        const StepParams<T, S> P)
+{
+    const long long nyz = (long long)P.ny * P.nz;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 2 * nyz) return;
+    const int side = int(q / nyz);
+    const long long o = q % nyz;
+    const int j = int(o % P.ny) + 1, k = int(o / P.ny) + 1;
+    const AdjRows R = adj_rows(j, k, P.nx, P.ny, P.nz);
+    adj_ghost_pops<T, S>(LX, LY, LZ, P, R, adj_nface(0, P.nx, P.ny, P.nz), adj_nface(1, P.nx, P.ny, P.nz), side,
+                         GH, o);
+}
+
+template <class T, class S, int p>
+__device__ __forceinline__ void adj_mu_pop(T mu[NPOP], const T *__restrict__ LX, const T *__restrict__ LY,
+                                           const T *__restrict__ LZ, const T *__restrict__ GH,
+                                           const S *__restrict__ lam_next, const StepParams<T, S> &P,
+                                           const AdjRows &R, int i, long long c, long long o, int Ix2,
+                                           bool x2_anchor, long long nfx, long long nfc)
+{
+    constexpr int ax = cx(p);
+    // second column of the y / z faces: i + cx (periodic image, or none past a wall)
+    int i2 = 0;
+    if (ax) {
+        i2 = i + ax;
+        if (P.periodic_x) i2 = i2 < 1 ? P.nx : (i2 > P.nx ? 1 : i2);
+        else if (i2 < 1 || i2 > P.nx) i2 = 0;
+    }
+    const AdjPop<p, T, S> A{LX, LY, LZ, P, R, nfx, nfc};
+    T m = T(4.0 / 3.0) * T(lam_next[p * P.ps + c]) + A.interior(i, Ix2, x2_anchor, i2);
+    if (!P.periodic_x && (i <= 2 || i >= P.nx - 1)) {
+        // wall ghosts: g0 = q0 fb1 + (1-q0) fb2, g_{nx+1} = q1 fb_nx + (1-q1) fb_{nx-1}
+        const long long nyz = (long long)P.ny * P.nz;
+        const T g0 = GH[(long long)p * nyz + o], g1 = GH[(long long)(NPOP + p) * nyz + o];
+        if (i == 1) m += P.q0 * g0;
+        if (i == 2) m += (T(1) - P.q0) * g0;
+        if (i == P.nx) m += P.q1 * g1;
+        if (i == P.nx - 1) m += (T(1) - P.q1) * g1;
+    }
+    mu[p] = m;
+}
+
+template <class T, class S, int p = 0>
+__device__ __forceinline__ void adj_mu_all(T mu[NPOP], const T *__restrict__ LX, const T *__restrict__ LY,
+                                           const T *__restrict__ LZ, const T *__restrict__ GH,
+                                           const S *__restrict__ lam_next, const StepParams<T, S> &P,
+                                           const AdjRows &R, int i, long long c, long long o, int Ix2,
+                                           bool x2_anchor, long long nfx, long long nfc)
+{
+    adj_mu_pop<T, S, p>(mu, LX, LY, LZ, GH, lam_next, P, R, i, c, o, Ix2, x2_anchor, nfx, nfc);
+    if constexpr (p + 1 < NPOP)
+        adj_mu_all<T, S, p + 1>(mu, LX, LY, LZ, GH, lam_next, P, R, i, c, o, Ix2, x2_anchor, nfx, nfc);
 }
 
 // mu = 4/3 lam' + (G^T L^T lamv); lam = (dA/df)^T mu - 1/3 lam'.
@@ -369,24 +455,22 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
                                                          const T *__restrict__ LZ, S *__restrict__ lam_out,
                                                          const T *__restrict__ LFX, const T *__restrict__ LFY,
                                                          const T *__restrict__ LFZ, double *__restrict__ dphi,
-                                                         const StepParams<T, S> P)
+                                                         const T *__restrict__ GH, const StepParams<T, S> P)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y + 1, k = blockIdx.z + 1;
     if (i > P.nx) return;
     const long long c = ((long long)(k - 1) * P.ny + (j - 1)) * P.pitch + (i - 1);
     T mu[NPOP];
-#pragma unroll
-    for (int p = 0; p < NPOP; ++p) {
-        T m = T(4.0 / 3.0) * T(lam_next[p * P.ps + c]) + adj_received(LX, LY, LZ, P, p, i, j, k);
-        if (!P.periodic_x) {
-            // wall ghosts: g0 = q0 fb1 + (1-q0) fb2, g_{nx+1} = q1 fb_nx + (1-q1) fb_{nx-1}
-            if (i == 1) m += P.q0 * adj_received(LX, LY, LZ, P, p, 0, j, k);
-            if (i == 2) m += (T(1) - P.q0) * adj_received(LX, LY, LZ, P, p, 0, j, k);
-            if (i == P.nx) m += P.q1 * adj_received(LX, LY, LZ, P, p, P.nx + 1, j, k);
-            if (i == P.nx - 1) m += (T(1) - P.q1) * adj_received(LX, LY, LZ, P, p, P.nx + 1, j, k);
-        }
-        mu[p] = m;
+    {
+        const AdjRows R = adj_rows(j, k, P.nx, P.ny, P.nz);
+        const long long nfx = adj_nface(0, P.nx, P.ny, P.nz), nfc = adj_nface(1, P.nx, P.ny, P.nz);
+        // second x face holding column i: face i-1 ("other" column), face 0 (anchor) at a wall,
+        // face nx ("other") for i = 1 when periodic
+        const bool wall1 = !P.periodic_x && i == 1;
+        const int Ix2 = i == 1 ? (P.periodic_x ? P.nx : 0) : i - 1;
+        const long long o = (long long)(k - 1) * P.ny + (j - 1);
+        adj_mu_all<T, S>(mu, LX, LY, LZ, GH, lam_next, P, R, i, c, o, Ix2, wall1, nfx, nfc);
     }
     // stage (a) transpose at this cell
     T v[NPOP];

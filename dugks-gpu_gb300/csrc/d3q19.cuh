@@ -25,6 +25,12 @@ __host__ __device__ constexpr int cz(int p)
 }
 __host__ __device__ constexpr int cc(int axis, int p) { return axis == 0 ? cx(p) : axis == 1 ? cy(p) : cz(p); }
 
+// Representative population of the class of p with the same c_x: 1 (c_x > 0),
+// 2 (c_x < 0), 3 (c_x = 0).  The x-interpolation weight tables depend on p
+// only through c_x, so reading them at the representative lets the compiler
+// share one load per class.
+__host__ __device__ constexpr int xrep(int p) { return cx(p) > 0 ? 1 : (cx(p) < 0 ? 2 : 3); }
+
 // opposite population (src/lbm_d3q19.cu:15)
 __host__ __device__ constexpr int opp(int p)
 {

@@ -336,7 +336,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ay = cy(p), az = cz(p);
-            const int rp = cx(p) > 0 ? 1 : (cx(p) < 0 ? 2 : 3);
+            const int rp = xrep(p);
             const T om = __ldg(xw + 2 * rp), m = __ldg(xw + 2 * rp + 1);
             const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
             const int kt = az > 0 ? km : (az < 0 ? kp : kc);
@@ -370,7 +370,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
             const int io = i - ax;
             const int kt = az > 0 ? km : (az < 0 ? kp : kc);
             T txo = T(1), txm = T(0);
-            if (ax) { txo = __ldg(tw + (ax > 0 ? 2 : 4)); txm = __ldg(tw + (ax > 0 ? 3 : 5)); }  // rep. 1 / 2
+            if (ax) { txo = __ldg(tw + 2 * xrep(p)); txm = __ldg(tw + 2 * xrep(p) + 1); }
             T x00 = R(p, rA, i), x01 = R(p, rB, i);
             if (ax) {
                 x00 = lerp2(txo, txm, x00, R(p, rA, io));
@@ -400,7 +400,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
             const int io = i - ax;
             const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
             T txo = T(1), txm = T(0);
-            if (ax) { txo = __ldg(tw + (ax > 0 ? 2 : 4)); txm = __ldg(tw + (ax > 0 ? 3 : 5)); }  // rep. 1 / 2
+            if (ax) { txo = __ldg(tw + 2 * xrep(p)); txm = __ldg(tw + 2 * xrep(p) + 1); }
             T x00 = R(p, rA, i), x10 = R(p, rB, i);
             if (ax) {
                 x00 = lerp2(txo, txm, x00, R(p, rA, io));

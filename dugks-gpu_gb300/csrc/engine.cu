@@ -110,6 +110,7 @@ struct dg_ctx {
     int prec = DG_PREC_FP64;
     int mesh = 0;           // 0 uniform, 1 tanh, 2 file
     int recon = 0;          // 0 trilinear
+    int stochastic = 1;     // BF16 form: stochastic rounding of the stored deviations
     double mesh_alpha = 0.85;
     std::string mesh_file;
     // derived
@@ -209,6 +210,10 @@ int load_config(dg_ctx *h, const ConfigFile &cf)
     else return h->fail(DG_ERR_CONFIG, "config key 'mesh': expected uniform, tanh or file, got '" + mesh + "'");
     if (!cf.opt_double("mesh_alpha", 0.85, h->mesh_alpha, e)) return h->fail(DG_ERR_CONFIG, e);
     h->mesh_file = cf.opt_string("mesh_file", "mesh.txt");
+    const std::string rounding = cf.opt_string("rounding", "stochastic");
+    if (rounding == "stochastic") h->stochastic = 1;
+    else if (rounding == "nearest") h->stochastic = 0;
+    else return h->fail(DG_ERR_CONFIG, "config key 'rounding': expected stochastic or nearest, got '" + rounding + "'");
     const std::string recon = cf.opt_string("recon", "trilinear");
     if (recon == "trilinear") h->recon = 0;
     else if (recon == "gradient") h->recon = 1;
@@ -422,6 +427,15 @@ void set_codec<float, __nv_bfloat16>(const dg_ctx *h, Codec<float, __nv_bfloat16
     }
 }
 
+// per-step stochastic-rounding seed of the BF16 form (other forms: nothing)
+template <class T, class S>
+void set_round_seed(const dg_ctx *, Codec<T, S> &, int) {}
+template <>
+void set_round_seed<float, __nv_bfloat16>(const dg_ctx *h, Codec<float, __nv_bfloat16> &c, int istep)
+{
+    c.sr_seed = h->stochastic ? (mix32(unsigned(istep)) | 1u) : 0u;
+}
+
 template <class T, class S>
 StepParams<T, S> params_for(const dg_ctx *h, int istep)
 {
@@ -466,6 +480,7 @@ int step_form(dg_ctx *h, int istep0, int n, cudaEvent_t *ev)
     if (ev) CK(cudaEventRecord(ev[0], h->stream), "event record");
     for (int s = 0; s < n; ++s) {
         if (h->perturb && s > 0) P = params_for<T, S>(h, istep0 + s);
+        set_round_seed<T, S>(h, P.codec, istep0 + s);
         CK(K::fbar(f, fb, P, h->stream), "stage (a) launch");
         if (ev) CK(cudaEventRecord(ev[2 * s + 1], h->stream), "event record");
         CK(K::flux(fb, f, f, P, h->recon, h->have_tmap ? &h->tmap : nullptr, h->stream), "flux launch");
@@ -608,9 +623,11 @@ int adjoint_form(dg_ctx *h, int istep, const void *f_n, const void *lam_next, vo
     using K = Kern<T, S>;
     if (!std::is_same<T, S>::value) return h->fail(DG_ERR_UNSUPPORTED, "the adjoint exists for the fp64 and fp32 forms");
     if (!h->adj) {
-        // 19 adjoint values and one dJ/dF (force-field face term) per face
+        // 19 adjoint values and one dJ/dF (force-field face term) per face, then the
+        // wall-ghost sums (2 * 19 per row and plane)
         const long long n = adj_nface(0, h->nx, h->ny, h->nz) + 2 * adj_nface(1, h->nx, h->ny, h->nz);
-        CK(cudaMalloc(&h->adj, size_t(n) * (NPOP + 1) * sizeof(T)), "cudaMalloc (adjoint scratch)");
+        const long long ng = 2LL * NPOP * h->ny * h->nz;
+        CK(cudaMalloc(&h->adj, (size_t(n) * (NPOP + 1) + size_t(ng)) * sizeof(T)), "cudaMalloc (adjoint scratch)");
     }
     if (h->ffield && !h->dphi) {
         CK(cudaMalloc(&h->dphi, h->ncell() * sizeof(double)), "cudaMalloc (field gradient)");

@@ -143,8 +143,13 @@ cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_o
         adj_face_kernel<T, S, 2><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LZ, LFZ, P);
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
+        T *GH = LFZ + nfc;  // wall-ghost sums, 2 * 19 * ny * nz
+        if (!P.periodic_x) {
+            const long long ng = 2LL * P.ny * P.nz;
+            adj_ghost_kernel<T, S><<<unsigned((ng + 127) / 128), 128, 0, st>>>(LX, LY, LZ, GH, P);
+        }
         dim3 grid((P.nx + 127) / 128, P.ny, P.nz);
-        adj_gather_kernel<T, S><<<grid, 128, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, LFX, LFY, LFZ, dphi, P);
+        adj_gather_kernel<T, S><<<grid, 128, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, LFX, LFY, LFZ, dphi, GH, P);
         return cudaGetLastError();
     }
 }

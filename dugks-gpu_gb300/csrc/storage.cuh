@@ -4,6 +4,11 @@
 //   Codec<float, __half>, Codec<float, __nv_bfloat16>: 16-bit deviations from
 //       the rest-state equilibrium, d_p = (f_p - w_p) / s_p, with one scale s_p
 //       per population; decoded and re-encoded in FP32 (the mixed form).
+//       BF16 (8 significant bits) is written with stochastic rounding when
+//       sr_seed != 0: 16 hashed bits of (index, population, seed) are added
+//       below the BF16 mantissa before truncation, so the rounding error has
+//       zero mean and does not bias time averages; the seed changes every
+//       step and the result stays deterministic.
 #pragma once
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
@@ -26,8 +31,20 @@ struct DevCodec {
     float w[NPOP];    // rest-state equilibrium w_p (feq(rho=1, u=0))
     float s[NPOP];    // scale s_p
     float is[NPOP];   // 1 / s_p
+    unsigned sr_seed; // BF16: 0 round to nearest, else stochastic rounding with this seed
     static constexpr bool deviation = true;
 };
+
+// 32-bit integer mixer ("lowbias32", C. Wellons' hash-prospector, public domain)
+__host__ __device__ __forceinline__ unsigned mix32(unsigned x)
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
 
 template <>
 struct Codec<float, __half> : DevCodec<__half> {
@@ -65,7 +82,14 @@ struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
     }
     __device__ __forceinline__ void store(__nv_bfloat16 *a, long long idx, int p, float v) const
     {
-        a[idx] = __float2bfloat16_rn((v - w[p]) * is[p]);
+        const float d = (v - w[p]) * is[p];
+        if (sr_seed == 0) {
+            a[idx] = __float2bfloat16_rn(d);
+            return;
+        }
+        const unsigned r = mix32(unsigned(idx) * 19u + unsigned(p) + sr_seed * 0x9e3779b9u);
+        const unsigned u = __float_as_uint(d) + (r & 0xffffu);  // magnitude rounds up with probability = fraction
+        a[idx] = __ushort_as_bfloat16((unsigned short)(u >> 16));
     }
 };
 

@@ -83,6 +83,8 @@ def test_bad_extension_values():
     assert create(pydugks.make_config(mesh="cubic"))[0] == DG_ERR_CONFIG
     assert create(pydugks.make_config(mesh="tanh", mesh_alpha=1.5))[0] == DG_ERR_CONFIG
     assert create(pydugks.make_config(mesh="tanh", periods_x=1))[0] == DG_ERR_CONFIG
+    assert create(pydugks.make_config(precision="bf16", rounding="up"))[0] == DG_ERR_CONFIG
+    assert gpu_or_ok(create(pydugks.make_config(precision="bf16", rounding="nearest"))[0])
 
 
 def test_tiny_grid_rejected():
