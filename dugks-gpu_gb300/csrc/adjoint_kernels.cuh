@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
     if (AX == 0) {
         A = I == 0 ? 1 : I;
         Bc = I == 0 ? 0 : I + 1;
-        xwf = P.xw + (size_t)I * 38;
+        xwf = P.xw + I;
     }
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
         }
         if (AX == 0) {
             const int rp = xrep(p);
-            const T om = __ldg(xwf + 2 * rp), m = __ldg(xwf + 2 * rp + 1);
+            const T om = __ldg(xwf + (2 * rp) * P.xws), m = __ldg(xwf + (2 * rp + 1) * P.xws);
             auto xl = [&](int jj, int kk) { return lerp2(om, m, fb_at(fb, P, p, A, jj, kk), fb_at(fb, P, p, Bc, jj, kk)); };
             const T x00 = xl(j, k);
             T y00 = x00;
@@ -143,8 +143,8 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
         } else {
             T txo = T(1), txm = T(0);
             if (ax) {
-                txo = __ldg(P.txw + (size_t)i * 38 + 2 * xrep(p));
-                txm = __ldg(P.txw + (size_t)i * 38 + 2 * xrep(p) + 1);
+                txo = __ldg(P.txw + (2 * xrep(p)) * P.xws + i);
+                txm = __ldg(P.txw + (2 * xrep(p) + 1) * P.xws + i);
             }
             auto xt = [&](int jj, int kk) {
                 T a = fb_at(fb, P, p, i, jj, kk);
@@ -311,10 +311,10 @@ struct AdjPop {
     // x weight of face I: anchor (which = 0) or other column (which = 1)
     __device__ __forceinline__ T xw(int I, int which) const
     {
-        return p == 0 ? T(0.5) : __ldg(P.xw + (size_t)I * 38 + 2 * rp + which);
+        return p == 0 ? T(0.5) : __ldg(P.xw + (2 * rp + which) * P.xws + I);
     }
     // transverse x weight of the y / z faces at column i: own column (0) or column i - cx (1)
-    __device__ __forceinline__ T tw(int i, int which) const { return __ldg(P.txw + (size_t)i * 38 + 2 * rp + which); }
+    __device__ __forceinline__ T tw(int i, int which) const { return __ldg(P.txw + (2 * rp + which) * P.xws + i); }
     __device__ __forceinline__ T colsum(int i) const
     {
         const T tyo = p == 0 ? T(1) : P.ty_om, tym = P.ty_m, tzo = p == 0 ? T(1) : P.tz_om, tzm = P.tz_m;

@@ -61,8 +61,9 @@ struct StepParams {
     T q0, q1;                    // wall ghost extrapolation weights (2 on a uniform mesh)
     T g_idx, g_idy, g_idz;       // gradient reconstruction: 1/dx, 1/dy, 1/dz
     T g_i2dx, g_i2dy, g_i2dz;    // 1/(2dx), 1/(2dy), 1/(2dz)
-    const T *xw;                 // [(nx+1)*19*2] x-face normal (1-m, m); face I lies between cells I, I+1 (1-based)
-    const T *txw;                // [(nx+2)*19*2] transverse x (1-t, t) per column 0..nx+1
+    const T *xw;                 // [19*2][xws] x-face normal (1-m, m) of face I (between cells I, I+1, 1-based)
+    const T *txw;                // [19*2][xws] transverse x (1-t, t) per column 0..nx+1
+    int xws;                     // row stride of xw / txw (nx+2)
     const T *cxu;                // [nx+2] dt/dxx(i)
     const T *cxuf;               // [nx+2] fw1*dt/dxx(i)
     // perturbation forcing (src/dugks.cu:1086-1126) as separable factors
@@ -330,14 +331,14 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
         const int A = i == 0 ? 1 : i, B = i == 0 ? 0 : i + 1;
         // the x weights depend on p only through cx(p): read them at the
         // representative population (1: cx>0, 2: cx<0, 3: cx=0), one load per class
-        const T *xw = P.xw + (size_t)i * 38;
+        const T *xw = P.xw + i;
         const RI r00 = R.rb(jc, kc);
         v[0] = T(0.5) * (R(0, r00, A) + R(0, r00, B));
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ay = cy(p), az = cz(p);
             const int rp = xrep(p);
-            const T om = __ldg(xw + 2 * rp), m = __ldg(xw + 2 * rp + 1);
+            const T om = __ldg(xw + (2 * rp) * P.xws), m = __ldg(xw + (2 * rp + 1) * P.xws);
             const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
             const int kt = az > 0 ? km : (az < 0 ? kp : kc);
             const T x00 = lerp2(om, m, R(p, r00, A), R(p, r00, B));
@@ -363,14 +364,14 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
         // rows j (anchor) and j+1 (other); transverse x to column i - cx, z to plane k - cz
         const RI rA = R.rb(jc, kc), rB = R.rb(jp, kc);
         v[0] = T(0.5) * (R(0, rA, i) + R(0, rB, i));
-        const T *tw = P.txw + (size_t)i * 38;
+        const T *tw = P.txw + i;
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ax = cx(p), az = cz(p);
             const int io = i - ax;
             const int kt = az > 0 ? km : (az < 0 ? kp : kc);
             T txo = T(1), txm = T(0);
-            if (ax) { txo = __ldg(tw + 2 * xrep(p)); txm = __ldg(tw + 2 * xrep(p) + 1); }
+            if (ax) { txo = __ldg(tw + (2 * xrep(p)) * P.xws); txm = __ldg(tw + (2 * xrep(p) + 1) * P.xws); }
             T x00 = R(p, rA, i), x01 = R(p, rB, i);
             if (ax) {
                 x00 = lerp2(txo, txm, x00, R(p, rA, io));
@@ -393,14 +394,14 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
         // planes k (anchor) and k+1 (other); transverse x to i - cx, y to row j - cy
         const RI rA = R.rb(jc, kc), rB = R.rb(jc, kp);
         v[0] = T(0.5) * (R(0, rA, i) + R(0, rB, i));
-        const T *tw = P.txw + (size_t)i * 38;
+        const T *tw = P.txw + i;
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ax = cx(p), ay = cy(p);
             const int io = i - ax;
             const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
             T txo = T(1), txm = T(0);
-            if (ax) { txo = __ldg(tw + 2 * xrep(p)); txm = __ldg(tw + 2 * xrep(p) + 1); }
+            if (ax) { txo = __ldg(tw + (2 * xrep(p)) * P.xws); txm = __ldg(tw + (2 * xrep(p) + 1) * P.xws); }
             T x00 = R(p, rA, i), x10 = R(p, rB, i);
             if (ax) {
                 x00 = lerp2(txo, txm, x00, R(p, rA, io));
@@ -776,7 +777,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
     const bool hx = wr == 0 && lane < W - 1 && hj <= ny;
 
     for (int g = kb - 1; g <= kb + 2; ++g) issue(g);
-    T fzd[10], fzu[10], fx[10], fy[10];
+    T fzd[10], fzu[10], fx[10], fy[10], fo[NPOP];
     int buf = 0;
     wait(kb - 1);
     wait(kb);
@@ -789,6 +790,12 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
             face_fluxes<T, S, 2, RECON, FF>(P, R, ci, cj, k, fzu);
 #pragma unroll
             for (int s = 0; s < 10; ++s) ysh[buf][wr][s][lane] = fy[s];
+            // the cell's f-tilde, loaded before the barrier so its latency overlaps the exchange
+            if (cell) {
+                const long long c = ((long long)(k - 1) * ny + (gj - 1)) * P.pitch + (gi - 1);
+#pragma unroll
+                for (int p = 0; p < NPOP; ++p) fo[p] = P.codec.load(f_in, p * P.ps + c, p);
+            }
         } else {
             face_fluxes<T, S, 1, RECON, FF>(P, R, ci, j0 - 1, k, fy);
 #pragma unroll
@@ -816,8 +823,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
                 const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
 #pragma unroll
                 for (int p = 0; p < NPOP; ++p) {
-                    const T fo = P.codec.load(f_in, p * P.ps + c, p);
-                    T r = fma(R(p, cb, 0), c43, -(fo * c13));
+                    T r = fma(R(p, cb, 0), c43, -(fo[p] * c13));
                     if (cx(p)) {
                         const int s = flux_slot(0, p);
                         r = fma(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s], r);

@@ -283,8 +283,11 @@ void make_tables(const dg_ctx *h, const RefCoef<R> &c, std::vector<T> &xw, std::
     const int nx = h->nx, ny = h->ny, nz = h->nz;
     const bool st = h->mesh != 0;
     const R hdt = c.hdt, dx = c.dx;
-    xw.assign(size_t(nx + 1) * 38, T(0));
-    txw.assign(size_t(nx + 2) * 38, T(0));
+    // population-major rows [2p + (0: 1-w, 1: w)][column], so that lanes of a warp
+    // (consecutive columns) read consecutive words
+    const size_t xs = size_t(nx + 2);
+    xw.assign(xs * 38, T(0));
+    txw.assign(xs * 38, T(0));
     cxu.assign(nx + 2, T(0));
     for (int p = 1; p < 19; ++p) {
         const int cxp = dg::cx(p);
@@ -303,8 +306,8 @@ void make_tables(const dg_ctx *h, const RefCoef<R> &c, std::vector<T> &xw, std::
                     m = (di / 2 - hdt * cxp) / (R(0.5) * di + R(0.5) * dn);
                 }
             }
-            xw[size_t(I) * 38 + 2 * p] = T(R(1 - m));
-            xw[size_t(I) * 38 + 2 * p + 1] = T(m);
+            xw[size_t(2 * p) * xs + I] = T(R(1 - m));
+            xw[size_t(2 * p + 1) * xs + I] = T(m);
         }
         if (cxp != 0) {
             for (int gi = 1; gi <= nx; ++gi) {
@@ -313,8 +316,8 @@ void make_tables(const dg_ctx *h, const RefCoef<R> &c, std::vector<T> &xw, std::
                     t = std::fabs((-hdt * cxp) / dx);  // src/dugks.cu:827 with fabs at 850
                 else
                     t = std::fabs((-hdt * cxp) / (R(0.5) * R(h->dxx[gi]) + R(0.5) * R(h->dxx[gi - cxp])));  // dugks.cuf:595
-                txw[size_t(gi) * 38 + 2 * p] = T(R(1 - t));
-                txw[size_t(gi) * 38 + 2 * p + 1] = T(t);
+                txw[size_t(2 * p) * xs + gi] = T(R(1 - t));
+                txw[size_t(2 * p + 1) * xs + gi] = T(t);
             }
         }
     }
@@ -400,6 +403,7 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     }
     const char *base = static_cast<const char *>(h->tab);
     P.xw = reinterpret_cast<const T *>(base + h->tab_off[0]);
+    P.xws = h->nx + 2;
     P.txw = reinterpret_cast<const T *>(base + h->tab_off[1]);
     P.cxu = reinterpret_cast<const T *>(base + h->tab_off[2]);
     P.cxuf = reinterpret_cast<const T *>(base + h->tab_off[6]);

@@ -33,12 +33,31 @@ int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0, MB, false>, 32 * W, 0);
     occ = std::max(occ, 1);
     const long long cols = (long long)((P.nx + 31) / 32) * ((P.ny + W - 2) / (W - 1));
-    const long long want = 4LL * sms * occ;
-    long long nchunks = (want + cols - 1) / cols;
-    nchunks = std::max(1LL, std::min<long long>(nchunks, P.nz));
-    // at least 8 planes per chunk keeps the extra bottom-face evaluation below 1/8
-    nchunks = std::min<long long>(nchunks, std::max(1, P.nz / 8));
-    return int((P.nz + nchunks - 1) / nchunks);
+    const long long slots = (long long)sms * occ;
+    // Pick the z chunking: every chunk re-evaluates one bottom z face (1/(3k) of
+    // the face work for k planes) and refills the plane pipeline (about half a
+    // plane), and the last wave of CTAs may be partly empty; maximise
+    // (useful waves / launched waves) * (1 - 1/(3k)) * (1 - 1/(2k)) over chunk
+    // lengths k >= 4, keeping at least two waves where the grid allows it so
+    // that the scheduler can even out tiles of unequal work (partial rows).
+    const int kmin = std::min(P.nz, 4);
+    const long long max_chunks = (P.nz + kmin - 1) / kmin;
+    const double min_waves = std::min(2.0, double(cols * max_chunks) / double(slots));
+    int best_k = P.nz;
+    double best = -1.0;
+    for (int k = kmin; k <= P.nz; ++k) {
+        const long long nch = (P.nz + k - 1) / k;
+        if (k > kmin && (P.nz + k - 2) / (k - 1) == nch) continue;  // same chunk count as k-1
+        const double waves = double(cols * nch) / double(slots);
+        if (waves < min_waves - 1e-9) break;  // fewer chunks only lower the wave count further
+        const double fill = waves / std::ceil(waves);
+        const double score = fill * (1.0 - 1.0 / (3.0 * k)) * (1.0 - 0.5 / k) * std::min(1.0, waves);
+        if (score > best + 1e-9) {
+            best = score;
+            best_k = k;
+        }
+    }
+    return best_k;
 }
 
 // one launch of the flux kernel variant <RECON, FF>
