@@ -313,6 +313,8 @@ struct FbRead {
     {
         return codec.load_nc(fb, p * ps + row + col, p);
     }
+    __device__ __forceinline__ T raw(int p, long long row, int col) const { return codec.raw_nc(fb, p * ps + row + col); }
+    __device__ __forceinline__ T dec(int p, T x) const { return codec.dec(p, x); }
 };
 
 // 19 reconstructed values of one face, trilinear characteristic interpolation
@@ -324,7 +326,11 @@ template <class T, class S, int AX, class RD>
 __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R, int i, int j, int k, T v[NPOP])
 {
     using RI = decltype(R.rb(0, 0));
-    // j, k are stored indices (ghost rows / planes 0 and n+1 hold the periodic images)
+    // j, k are stored indices (ghost rows / planes 0 and n+1 hold the periodic images).
+    // The stencil is read undecoded (R.raw) and each face value decoded once
+    // (R.dec): the interpolation is affine with weights summing to one, so for
+    // the 16-bit deviation forms s (sum w d) + w_eq equals sum w (s d + w_eq);
+    // for FP64 / FP32 both are the identity and the arithmetic is unchanged.
     const int jm = j - 1, jp = j + 1, jc = j;
     const int km = k - 1, kp = k + 1, kc = k;
     if (AX == 0) {
@@ -333,7 +339,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
         // representative population (1: cx>0, 2: cx<0, 3: cx=0), one load per class
         const T *xw = P.xw + i;
         const RI r00 = R.rb(jc, kc);
-        v[0] = T(0.5) * (R(0, r00, A) + R(0, r00, B));
+        v[0] = R.dec(0, T(0.5) * (R.raw(0, r00, A) + R.raw(0, r00, B)));
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ay = cy(p), az = cz(p);
@@ -341,29 +347,29 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
             const T om = __ldg(xw + (2 * rp) * P.xws), m = __ldg(xw + (2 * rp + 1) * P.xws);
             const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
             const int kt = az > 0 ? km : (az < 0 ? kp : kc);
-            const T x00 = lerp2(om, m, R(p, r00, A), R(p, r00, B));
+            const T x00 = lerp2(om, m, R.raw(p, r00, A), R.raw(p, r00, B));
             T y00 = x00;
             if (ay) {
                 const RI r10 = R.rb(jt, kc);
-                y00 = lerp2(P.ty_om, P.ty_m, x00, lerp2(om, m, R(p, r10, A), R(p, r10, B)));
+                y00 = lerp2(P.ty_om, P.ty_m, x00, lerp2(om, m, R.raw(p, r10, A), R.raw(p, r10, B)));
             }
             if (az) {
                 const RI r01 = R.rb(jc, kt);
-                const T x10 = lerp2(om, m, R(p, r01, A), R(p, r01, B));
+                const T x10 = lerp2(om, m, R.raw(p, r01, A), R.raw(p, r01, B));
                 T y11 = x10;
                 if (ay) {
                     const RI r11 = R.rb(jt, kt);
-                    y11 = lerp2(P.ty_om, P.ty_m, x10, lerp2(om, m, R(p, r11, A), R(p, r11, B)));
+                    y11 = lerp2(P.ty_om, P.ty_m, x10, lerp2(om, m, R.raw(p, r11, A), R.raw(p, r11, B)));
                 }
-                v[p] = lerp2(P.tz_om, P.tz_m, y00, y11);
+                v[p] = R.dec(p, lerp2(P.tz_om, P.tz_m, y00, y11));
             } else {
-                v[p] = y00;
+                v[p] = R.dec(p, y00);
             }
         }
     } else if (AX == 1) {
         // rows j (anchor) and j+1 (other); transverse x to column i - cx, z to plane k - cz
         const RI rA = R.rb(jc, kc), rB = R.rb(jp, kc);
-        v[0] = T(0.5) * (R(0, rA, i) + R(0, rB, i));
+        v[0] = R.dec(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
         const T *tw = P.txw + i;
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
@@ -372,28 +378,28 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
             const int kt = az > 0 ? km : (az < 0 ? kp : kc);
             T txo = T(1), txm = T(0);
             if (ax) { txo = __ldg(tw + (2 * xrep(p)) * P.xws); txm = __ldg(tw + (2 * xrep(p) + 1) * P.xws); }
-            T x00 = R(p, rA, i), x01 = R(p, rB, i);
+            T x00 = R.raw(p, rA, i), x01 = R.raw(p, rB, i);
             if (ax) {
-                x00 = lerp2(txo, txm, x00, R(p, rA, io));
-                x01 = lerp2(txo, txm, x01, R(p, rB, io));
+                x00 = lerp2(txo, txm, x00, R.raw(p, rA, io));
+                x01 = lerp2(txo, txm, x01, R.raw(p, rB, io));
             }
             const T y00 = lerp2(P.yn_om[p], P.yn_m[p], x00, x01);
             if (az) {
                 const RI sA = R.rb(jc, kt), sB = R.rb(jp, kt);
-                T x10 = R(p, sA, i), x11 = R(p, sB, i);
+                T x10 = R.raw(p, sA, i), x11 = R.raw(p, sB, i);
                 if (ax) {
-                    x10 = lerp2(txo, txm, x10, R(p, sA, io));
-                    x11 = lerp2(txo, txm, x11, R(p, sB, io));
+                    x10 = lerp2(txo, txm, x10, R.raw(p, sA, io));
+                    x11 = lerp2(txo, txm, x11, R.raw(p, sB, io));
                 }
-                v[p] = lerp2(P.tz_om, P.tz_m, y00, lerp2(P.yn_om[p], P.yn_m[p], x10, x11));
+                v[p] = R.dec(p, lerp2(P.tz_om, P.tz_m, y00, lerp2(P.yn_om[p], P.yn_m[p], x10, x11)));
             } else {
-                v[p] = y00;
+                v[p] = R.dec(p, y00);
             }
         }
     } else {
         // planes k (anchor) and k+1 (other); transverse x to i - cx, y to row j - cy
         const RI rA = R.rb(jc, kc), rB = R.rb(jc, kp);
-        v[0] = T(0.5) * (R(0, rA, i) + R(0, rB, i));
+        v[0] = R.dec(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
         const T *tw = P.txw + i;
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
@@ -402,23 +408,23 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
             const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
             T txo = T(1), txm = T(0);
             if (ax) { txo = __ldg(tw + (2 * xrep(p)) * P.xws); txm = __ldg(tw + (2 * xrep(p) + 1) * P.xws); }
-            T x00 = R(p, rA, i), x10 = R(p, rB, i);
+            T x00 = R.raw(p, rA, i), x10 = R.raw(p, rB, i);
             if (ax) {
-                x00 = lerp2(txo, txm, x00, R(p, rA, io));
-                x10 = lerp2(txo, txm, x10, R(p, rB, io));
+                x00 = lerp2(txo, txm, x00, R.raw(p, rA, io));
+                x10 = lerp2(txo, txm, x10, R.raw(p, rB, io));
             }
             T y00 = x00, y11 = x10;
             if (ay) {
                 const RI sA = R.rb(jt, kc), sB = R.rb(jt, kp);
-                T x01 = R(p, sA, i), x11 = R(p, sB, i);
+                T x01 = R.raw(p, sA, i), x11 = R.raw(p, sB, i);
                 if (ax) {
-                    x01 = lerp2(txo, txm, x01, R(p, sA, io));
-                    x11 = lerp2(txo, txm, x11, R(p, sB, io));
+                    x01 = lerp2(txo, txm, x01, R.raw(p, sA, io));
+                    x11 = lerp2(txo, txm, x11, R.raw(p, sB, io));
                 }
                 y00 = lerp2(P.ty_om, P.ty_m, x00, x01);
                 y11 = lerp2(P.ty_om, P.ty_m, x10, x11);
             }
-            v[p] = lerp2(P.zn_om[p], P.zn_m[p], y00, y11);
+            v[p] = R.dec(p, lerp2(P.zn_om[p], P.zn_m[p], y00, y11));
         }
     }
 }
@@ -696,6 +702,8 @@ struct SmemRead {
     {
         return codec.load_s(ring, p * POPS + row + col, p);
     }
+    __device__ __forceinline__ T raw(int p, int row, int col) const { return codec.raw_s(ring, p * POPS + row + col); }
+    __device__ __forceinline__ T dec(int p, T x) const { return codec.dec(p, x); }
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)

@@ -23,6 +23,10 @@ struct Codec {
     __device__ __forceinline__ T load_nc(const S *a, long long idx, int) const { return T(__ldg(a + idx)); }
     __device__ __forceinline__ T load_s(const S *a, int idx, int) const { return T(a[idx]); }
     __device__ __forceinline__ void store(S *a, long long idx, int, T v) const { a[idx] = S(v); }
+    // undecoded reads and the decode of a value affine in them (identity here)
+    __device__ __forceinline__ T raw_nc(const S *a, long long idx) const { return T(__ldg(a + idx)); }
+    __device__ __forceinline__ T raw_s(const S *a, int idx) const { return T(a[idx]); }
+    __device__ __forceinline__ T dec(int, T x) const { return x; }
     static constexpr bool deviation = false;
 };
 
@@ -64,6 +68,9 @@ struct Codec<float, __half> : DevCodec<__half> {
     {
         a[idx] = __float2half_rn((v - w[p]) * is[p]);
     }
+    __device__ __forceinline__ float raw_nc(const __half *a, long long idx) const { return __half2float(__ldg(a + idx)); }
+    __device__ __forceinline__ float raw_s(const __half *a, int idx) const { return __half2float(a[idx]); }
+    __device__ __forceinline__ float dec(int p, float x) const { return fmaf(s[p], x, w[p]); }
 };
 
 template <>
@@ -91,6 +98,12 @@ struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
         const unsigned u = __float_as_uint(d) + (r & 0xffffu);  // magnitude rounds up with probability = fraction
         a[idx] = __ushort_as_bfloat16((unsigned short)(u >> 16));
     }
+    __device__ __forceinline__ float raw_nc(const __nv_bfloat16 *a, long long idx) const
+    {
+        return __bfloat162float(__ldg(a + idx));
+    }
+    __device__ __forceinline__ float raw_s(const __nv_bfloat16 *a, int idx) const { return __bfloat162float(a[idx]); }
+    __device__ __forceinline__ float dec(int p, float x) const { return fmaf(s[p], x, w[p]); }
 };
 
 }  // namespace dg
