@@ -215,25 +215,32 @@ def cpu_baseline(args, budget_s=12.0):
 
 
 def reference_gpu(args, k=10):
-    """The reference's own CUDA-C kernels (oracle/_ref cubin) on the uniform-mesh
-    variant of the same grid (the reference has no stretched mesh)."""
+    """The reference's own CUDA-C kernels (oracle/_ref cubins, FP64 and its
+    PREC4 FP32 build) on the uniform-mesh variant of the same grid (the
+    reference has no stretched mesh), parameters parsed from the same
+    config.txt text as the reference would (std::stof)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import numpy as np
     import pyoracle
     if not pyoracle.ref_cubins_present():
         return None
-    nx, ny, nz = (int(v) for v in args.grid.split(","))
+    cfg, _, (nx, ny, nz) = workload(args, "fp64")
+    kv = dict(l.split("=", 1) for l in cfg.splitlines() if "=" in l)
+    st = lambda key: float(np.float32(float(kv[key])))  # noqa: E731
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     from seeded import seeded_state  # noqa: E402
-    f = pyoracle.to_ghosted(seeded_state(nx, ny, nz, seed=0, umax=0.05, eps=0.001))
-    ms = pyoracle.ref_run(f, nx, ny, nz, 0.5, float(nx), float(np.float32(268.0826)), float(np.float32(804.2477)),
-                          float(np.float32(0.00227007141)), (0.0, 0.0, float(np.float32(6.36918888e-07))),
-                          periods=(0, 1, 1), istep0=1, nsteps=2, prec=0)
-    ms = pyoracle.ref_run(f, nx, ny, nz, 0.5, float(nx), float(np.float32(268.0826)), float(np.float32(804.2477)),
-                          float(np.float32(0.00227007141)), (0.0, 0.0, float(np.float32(6.36918888e-07))),
-                          periods=(0, 1, 1), istep0=3, nsteps=k, prec=0)
-    return {"value": nx * ny * nz / (ms / 1e3) / 1e6, "unit": "MLUPS", "ms_per_step": ms, "steps": k,
-            "what": "reference src/dugks.cu kernels (unmodified, nvcc sm_103a), FP64, uniform-mesh variant of the grid"}
+    out = {}
+    for prec, name in ((0, "fp64"), (1, "fp32")):
+        f = pyoracle.to_ghosted(seeded_state(nx, ny, nz, seed=0, umax=0.05, eps=0.001))
+        common = dict(periods=(0, 1, 1), prec=prec)
+        args_ = (f, nx, ny, nz, st("CFL"), st("xwidth"), st("ywidth"), st("zwidth"), st("visc"),
+                 (st("ambient_fx"), st("ambient_fy"), st("ambient_fz")))
+        pyoracle.ref_run(*args_, istep0=1, nsteps=2, **common)
+        ms = pyoracle.ref_run(*args_, istep0=3, nsteps=k, **common)
+        out[name] = {"value": nx * ny * nz / (ms / 1e3) / 1e6, "unit": "MLUPS", "ms_per_step": ms, "steps": k}
+    out["what"] = ("reference src/dugks.cu kernels (unmodified, nvcc sm_103a; FP32 = its PREC4 build), "
+                   "uniform-mesh variant of the grid, CUDA events around dugks_step's launches")
+    return out
 
 
 def main_reference(args):

@@ -45,14 +45,6 @@ __device__ __forceinline__ void adj_accum(AdjJac<T> &J, int p, T lam, T r, T u, 
 }
 
 template <class T, class S>
-__device__ __forceinline__ T fb_at(const S *fb, const StepParams<T, S> &P, int p, int gi, int gj, int gk)
-{
-    // stored indices 0..n+1: the ghost layer written by fb_ghost_kernel holds the images
-    const long long row = ((long long)gk * (P.ny + 2) + gj) * P.pitch_b;
-    return P.codec.load_nc(fb, p * P.ps_b + row + gi, p);
-}
-
-template <class T, class S>
 __device__ __forceinline__ T lam_at(const S *lam, const StepParams<T, S> &P, int p, int gi, int gj, int gk)
 {
     const long long c = ((long long)(gk - 1) * P.ny + (gj - 1)) * P.pitch + (gi - 1);
@@ -76,99 +68,21 @@ __host__ __device__ inline long long adj_cell(int i, int j, int k, int nx, int n
     return ((long long)(k - 1) * ny + (j - 1)) * nx + (i - 1);
 }
 
-// Per-face adjoint: reconstruct the face values, take the flux adjoint from
-// the two adjacent cells' lam', apply (dphi/dv)^T and the bounce-back
-// transpose, store lamv[19] of the face (population-major, stride nface).
-template <class T, class S, int AX>
-__global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb, const S *__restrict__ lam_next,
-                                                       T *__restrict__ lamv, T *__restrict__ lamF_face,
-                                                       const StepParams<T, S> P)
+// Per-face adjoint: reconstruct the face values (the forward's face_tri with
+// reader RD), take the flux adjoint from the two adjacent cells' lam', apply
+// (dphi/dv)^T and the bounce-back transpose.  F: the face's first index (x
+// faces: I = 0..nx, between columns I and I+1; y / z faces: the column i);
+// j, k: row and plane (1-based).  lv: the 19 adjoint face values; lf: dJ/dF
+// of the face force along the field axis (0 without a field).
+template <class T, class S, int AX, class RD>
+__device__ __forceinline__ void adj_face_values(const StepParams<T, S> &P, const RD &R,
+                                                const S *__restrict__ lam_next, int F, int j, int k, T lv[NPOP],
+                                                T &lf)
 {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
-    const long long nface = adj_nface(AX, nx, ny, nz);
-    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nface) return;
-    int I = 0, i = 1, j, k;
-    if (AX == 0) {
-        I = int(q % (nx + 1));
-        const long long r = q / (nx + 1);
-        j = int(r % ny) + 1;
-        k = int(r / ny) + 1;
-        if (P.periodic_x && I == 0) {
-            for (int p = 0; p < NPOP; ++p) lamv[p * nface + q] = T(0);  // periodic: face 0 is face nx
-            if (lamF_face) lamF_face[q] = T(0);
-            return;
-        }
-    } else {
-        i = int(q % nx) + 1;
-        const long long r = q / nx;
-        j = int(r % ny) + 1;
-        k = int(r / ny) + 1;
-    }
-    // --- face values (same interpolation as face_values, global loads) ---
+    const int I = AX == 0 ? F : 0, i = AX == 0 ? 1 : F;
     T v[NPOP];
-    int A = i, Bc = i;  // x faces: anchor and other column
-    const T *xwf = nullptr;
-    if (AX == 0) {
-        A = I == 0 ? 1 : I;
-        Bc = I == 0 ? 0 : I + 1;
-        xwf = P.xw + I;
-    }
-#pragma unroll
-    for (int p = 0; p < NPOP; ++p) {
-        const int ax = cx(p), ay = cy(p), az = cz(p);
-        if (p == 0) {
-            T a, b;
-            if (AX == 0) { a = fb_at(fb, P, 0, A, j, k); b = fb_at(fb, P, 0, Bc, j, k); }
-            else if (AX == 1) { a = fb_at(fb, P, 0, i, j, k); b = fb_at(fb, P, 0, i, j + 1, k); }
-            else { a = fb_at(fb, P, 0, i, j, k); b = fb_at(fb, P, 0, i, j, k + 1); }
-            v[0] = T(0.5) * (a + b);
-            continue;
-        }
-        if (AX == 0) {
-            const int rp = xrep(p);
-            const T om = __ldg(xwf + (2 * rp) * P.xws), m = __ldg(xwf + (2 * rp + 1) * P.xws);
-            auto xl = [&](int jj, int kk) { return lerp2(om, m, fb_at(fb, P, p, A, jj, kk), fb_at(fb, P, p, Bc, jj, kk)); };
-            const T x00 = xl(j, k);
-            T y00 = x00;
-            if (ay) y00 = lerp2(P.ty_om, P.ty_m, x00, xl(j - ay, k));
-            if (az) {
-                const T x10 = xl(j, k - az);
-                T y11 = x10;
-                if (ay) y11 = lerp2(P.ty_om, P.ty_m, x10, xl(j - ay, k - az));
-                v[p] = lerp2(P.tz_om, P.tz_m, y00, y11);
-            } else {
-                v[p] = y00;
-            }
-        } else {
-            T txo = T(1), txm = T(0);
-            if (ax) {
-                txo = __ldg(P.txw + (2 * xrep(p)) * P.xws + i);
-                txm = __ldg(P.txw + (2 * xrep(p) + 1) * P.xws + i);
-            }
-            auto xt = [&](int jj, int kk) {
-                T a = fb_at(fb, P, p, i, jj, kk);
-                if (ax) a = lerp2(txo, txm, a, fb_at(fb, P, p, i - ax, jj, kk));
-                return a;
-            };
-            if (AX == 1) {
-                const T y00 = lerp2(P.yn_om[p], P.yn_m[p], xt(j, k), xt(j + 1, k));
-                if (az) {
-                    const T y11 = lerp2(P.yn_om[p], P.yn_m[p], xt(j, k - az), xt(j + 1, k - az));
-                    v[p] = lerp2(P.tz_om, P.tz_m, y00, y11);
-                } else {
-                    v[p] = y00;
-                }
-            } else {
-                T y00 = xt(j, k), y11 = xt(j, k + 1);
-                if (ay) {
-                    y00 = lerp2(P.ty_om, P.ty_m, y00, xt(j - ay, k));
-                    y11 = lerp2(P.ty_om, P.ty_m, y11, xt(j - ay, k + 1));
-                }
-                v[p] = lerp2(P.zn_om[p], P.zn_m[p], y00, y11);
-            }
-        }
-    }
+    face_tri<T, S, AX>(P, R, F, j, k, v);
     const bool lo = AX == 0 && !P.periodic_x && I == 0;
     const bool hi = AX == 0 && !P.periodic_x && I == nx;
     bounce_back(v, lo, hi);
@@ -178,14 +92,14 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) lamF[p] = T(0);
     if (AX == 0) {
-        const int L = I, R = I + 1 <= nx ? I + 1 : (P.periodic_x ? 1 : 0);
+        const int L = I, Rc = I + 1 <= nx ? I + 1 : (P.periodic_x ? 1 : 0);
         const T cl = L >= 1 ? __ldg(P.cxu + L) : T(0);
-        const T cr = R >= 1 ? __ldg(P.cxu + R) : T(0);
+        const T cr = Rc >= 1 ? __ldg(P.cxu + Rc) : T(0);
 #pragma unroll
         for (int s = 0; s < 10; ++s) {
             const int p = flux_pop(0, s);
             T a = T(0);
-            if (R >= 1) a += cr * lam_at(lam_next, P, p, R, j, k);
+            if (Rc >= 1) a += cr * lam_at(lam_next, P, p, Rc, j, k);
             if (L >= 1) a -= cl * lam_at(lam_next, P, p, L, j, k);
             lamF[p] = T(cx(p)) * a;
         }
@@ -208,12 +122,17 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
     // --- (dphi/dv)^T ---
     T r, jx, jy, jz;
     moments(v, r, jx, jy, jz);
-    const T inv = T(1) / r;
+    const T inv = recip(r);
     const T u0 = jx * inv, v0 = jy * inv, w0 = jz * inv;
     // face force: ambient plus the field averaged over the two cells
     T Ff[3] = {P.F[0], P.F[1], P.F[2]};
-    const T fadd = P.ffield ? face_field<T, S, AX>(P, AX == 0 ? I : i, j, k) : T(0);
-    if (P.ffield) Ff[P.ffaxis] += fadd;
+    const T fadd = P.ffield ? face_field<T, S, AX>(P, F, j, k) : T(0);
+    if (P.ffield) {
+        // add along the field axis with selects (no dynamically indexed local array)
+        Ff[0] += P.ffaxis == 0 ? fadd : T(0);
+        Ff[1] += P.ffaxis == 1 ? fadd : T(0);
+        Ff[2] += P.ffaxis == 2 ? fadd : T(0);
+    }
     const T hh = T(0.5) * P.hdt;
     T u = u0, vv = v0, w = w0, B = P.fw2;
     if (P.force_on || P.ffield) {
@@ -223,9 +142,11 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
         B = fma(-P.fw0x3, fma(Ff[0], u, fma(Ff[1], vv, Ff[2] * w)), P.fw2);
     }
     T fe[NPOP];
-    feq_all(r, u, vv, w, fe);
+    feq_face<T, AX>(r, u, vv, w, fe);
     AdjJac<T> Jc = {T(0), {T(0), T(0), T(0)}};
-    T Sc = T(0), Gq = T(0);  // parts of dJ/dF_face along the field axis
+    // with a field: L0 = sum lamF_p feq_p and L1 = sum lamF_p c_{a,p} feq_p along the field axis a
+    const int fax = P.ffaxis;
+    T L0 = T(0), L1 = T(0);
 #pragma unroll
     for (int s = 0; s < 10; ++s) {
         const int p = flux_pop(AX, s);
@@ -233,16 +154,24 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
         const T coef = B + P.fw0x3 * cfp;
         adj_accum(Jc, p, lamF[p], r, u, vv, w, coef, fe[p], P.fw0x3, Ff);
         if (P.ffield) {
-            const int ax = P.ffaxis;
-            const T ua = ax == 0 ? u : (ax == 1 ? vv : w);
-            const T ca = T(ax == 0 ? cx(p) : (ax == 1 ? cy(p) : cz(p)));
-            const T cu = T(cx(p)) * u + T(cy(p)) * vv + T(cz(p)) * w;
-            Sc += lamF[p] * (ca - ua - hh * Ff[ax]) * fe[p];
-            Gq += lamF[p] * coef * weight<T>(p) * r * (T(3) * ca + T(9) * cu * ca - T(3) * ua);
+            const T mf = lamF[p] * fe[p];
+            L0 += mf;
+            const int ca = fax == 0 ? cx(p) : (fax == 1 ? cy(p) : cz(p));
+            if (ca) L1 += ca > 0 ? mf : -mf;
         }
     }
-    if (lamF_face) lamF_face[q] = P.ffield ? P.fw0x3 * Sc + hh * Gq : T(0);
-    T lv[NPOP];
+    if (P.ffield) {
+        // dJ/dF_a = 3 fw0 sum lamF (c_a - u_a - hh F_a) feq + hh sum lamF coef d feq / d u_a
+        //         = 3 fw0 (L1 - (u_a + hh F_a) L0) + hh (Jc.G[a] + 3 fw0 F_a L0)
+        const T ua = fax == 0 ? u : (fax == 1 ? vv : w);
+        const T Fa = fax == 0 ? Ff[0] : (fax == 1 ? Ff[1] : Ff[2]);
+        const T Ga = fax == 0 ? Jc.G[0] : (fax == 1 ? Jc.G[1] : Jc.G[2]);
+        const T Sc = L1 - (ua + hh * Fa) * L0;
+        const T Gq = Ga + P.fw0x3 * Fa * L0;
+        lf = P.fw0x3 * Sc + hh * Gq;
+    } else {
+        lf = T(0);
+    }
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
         const T g = Jc.S0 + Jc.G[0] * (T(cx(p)) - u0) + Jc.G[1] * (T(cy(p)) - v0) + Jc.G[2] * (T(cz(p)) - w0);
@@ -257,15 +186,151 @@ __global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb,
         lv[1] += lv[2]; lv[2] = T(0); lv[7] += lv[10]; lv[10] = T(0); lv[9] += lv[8]; lv[8] = T(0);
         lv[11] += lv[14]; lv[14] = T(0); lv[13] += lv[12]; lv[12] = T(0);
     }
+}
+
+// One thread per face of orientation AX (f-bar-plus through L1), storing
+// lamv[19] of the face (population-major, stride nface) and dJ/dF.
+// only_x0: x faces I = 0 only (one thread per row and plane).
+template <class T, class S, int AX>
+__global__ void __launch_bounds__(128) adj_face_kernel(const S *__restrict__ fb, const S *__restrict__ lam_next,
+                                                       T *__restrict__ lamv, T *__restrict__ lamF_face,
+                                                       const StepParams<T, S> P, int only_x0)
+{
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const long long nface = adj_nface(AX, nx, ny, nz);
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long q;
+    int F, j, k;
+    if (AX == 0) {
+        if (only_x0) {
+            if (t >= (long long)ny * nz) return;
+            q = t * (nx + 1);
+        } else {
+            q = t;
+        }
+        if (q >= nface) return;
+        F = int(q % (nx + 1));
+        const long long r = q / (nx + 1);
+        j = int(r % ny) + 1;
+        k = int(r / ny) + 1;
+        if (P.periodic_x && F == 0) {
+            for (int p = 0; p < NPOP; ++p) lamv[p * nface + q] = T(0);  // periodic: face 0 is face nx
+            if (lamF_face) lamF_face[q] = T(0);
+            return;
+        }
+    } else {
+        q = t;
+        if (q >= nface) return;
+        F = int(q % nx) + 1;
+        const long long r = q / nx;
+        j = int(r % ny) + 1;
+        k = int(r / ny) + 1;
+    }
+    const FbRead<T, S> R{fb, P.ps_b, P.pitch_b, ny, nz, P.codec};
+    T lv[NPOP], lf;
+    adj_face_values<T, S, AX>(P, R, lam_next, F, j, k, lv, lf);
+    if (lamF_face) lamF_face[q] = lf;
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) lamv[p * nface + q] = lv[p];
+}
+
+// The three faces +x (I = i), +y (J = j) and +z (K = k) of every cell, with
+// f-bar-plus staged through the same 4-plane TMA ring as the forward flux
+// kernel: W warps, one row of 32 cells each, marching a chunk of z planes.
+// The box holds rows j0-1 .. j0+W (the stencil's transverse and +y rows).
+// x faces I = 0 are left to adj_face_kernel (only_x0).
+template <class T, class S, int W>
+constexpr size_t adj_faces_tma_smem_bytes()
+{
+    return 4 * size_t(SmemRead<T, S, W + 1>::STAGE_BYTES) + 4 * 8;
+}
+
+template <class T, class S, int W, int MINB>
+__global__ void __launch_bounds__(32 * W, MINB) adj_faces_tma_kernel(const __grid_constant__ CUtensorMap tmap,
+                                                                      const S *__restrict__ lam_next,
+                                                                      T *__restrict__ LX, T *__restrict__ LY,
+                                                                      T *__restrict__ LZ, T *__restrict__ LFX,
+                                                                      T *__restrict__ LFY, T *__restrict__ LFZ,
+                                                                      const StepParams<T, S> P, int kchunk)
+{
+    using RD = SmemRead<T, S, W + 1>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    S *ring = reinterpret_cast<S *>(smem);
+    unsigned long long *mbar = reinterpret_cast<unsigned long long *>(smem + 4 * RD::STAGE_BYTES);
+    constexpr unsigned TILE_BYTES = unsigned(NPOP * RD::POPS * sizeof(S));
+
+    const int lane = threadIdx.x, wr = threadIdx.y, tid = wr * 32 + lane;
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const int i0 = blockIdx.x * 32 + 1;
+    const int j0 = blockIdx.y * W + 1;
+    const int kb = blockIdx.z * kchunk + 1;
+    const int ke = min(kb + kchunk, nz + 1);
+    if (kb >= ke) return;
+    const RD R{ring, i0 - 1, j0 - 1, P.codec};
+
+    if (tid == 0) {
+        for (int s = 0; s < 4; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar + s)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int g) {  // stored plane g -> stage g & 3
+        if (tid == 0 && g <= ke) {
+            const unsigned bar = smem_u32(mbar + (g & 3));
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(TILE_BYTES)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+                "[%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(ring + (g & 3) * RD::STAGE)),
+                "l"(reinterpret_cast<unsigned long long>(&tmap)), "r"(i0 - 1), "r"(j0 - 1), "r"(g), "r"(0), "r"(bar)
+                : "memory");
+        }
+    };
+    unsigned phase = 0;
+    auto wait = [&](int g) {
+        const int s = g & 3;
+        if (!mbar_wait(smem_u32(mbar + s), (phase >> s) & 1u)) atomicOr(P.err, 1);
+        phase ^= 1u << s;
+    };
+
+    const int gi = i0 + lane, gj = j0 + wr;
+    const bool cell = gi <= nx && gj <= ny;
+    const long long nfx = adj_nface(0, nx, ny, nz), nfc = adj_nface(1, nx, ny, nz);
+    for (int g = kb - 1; g <= kb + 2; ++g) issue(g);
+    wait(kb - 1);
+    wait(kb);
+    for (int k = kb; k < ke; ++k) {
+        wait(k + 1);
+        if (cell) {
+            T lv[NPOP], lf;
+            const long long qx = adj_xface(gi, gj, k, nx, ny), qc = adj_cell(gi, gj, k, nx, ny);
+            adj_face_values<T, S, 0>(P, R, lam_next, gi, gj, k, lv, lf);
+            LFX[qx] = lf;
+#pragma unroll
+            for (int p = 0; p < NPOP; ++p) LX[p * nfx + qx] = lv[p];
+            adj_face_values<T, S, 1>(P, R, lam_next, gi, gj, k, lv, lf);
+            LFY[qc] = lf;
+#pragma unroll
+            for (int p = 0; p < NPOP; ++p) LY[p * nfc + qc] = lv[p];
+            adj_face_values<T, S, 2>(P, R, lam_next, gi, gj, k, lv, lf);
+            LFZ[qc] = lf;
+#pragma unroll
+            for (int p = 0; p < NPOP; ++p) LZ[p * nfc + qc] = lv[p];
+        }
+        __syncthreads();
+        issue(k + 3);  // plane k-1 (same stage) is no longer read
+    }
+    // every plane issued (g <= ke) has been waited for: no bulk copy is left in flight
 }
 
 // Row / plane offsets of the face arrays around one interior cell (the
 // periodic images in y and z folded in): x faces ((k-1)*ny + (j-1))*(nx+1),
 // y / z faces ((k-1)*ny + (j-1))*nx, for j-1..j+1 and k-1..k+1.
 struct AdjRows {
-    int x[3][3], c[3][3];  // [dk+1][dj+1]
+    int kx[3], jx[3];  // x faces: plane part ((k'-1)*ny)*(nx+1) and row part (j'-1)*(nx+1), k' = k-1..k+1
+    int kc[3], jc[3];  // y / z faces: the same with nx
+    __device__ __forceinline__ int x(int dk, int dj) const { return kx[dk] + jx[dj]; }  // [dk+1][dj+1]
+    __device__ __forceinline__ int c(int dk, int dj) const { return kc[dk] + jc[dj]; }
 };
 
 __device__ __forceinline__ AdjRows adj_rows(int j, int k, int nx, int ny, int nz)
@@ -274,13 +339,12 @@ __device__ __forceinline__ AdjRows adj_rows(int j, int k, int nx, int ny, int nz
     const int js[3] = {j == 1 ? ny : j - 1, j, j == ny ? 1 : j + 1};
     const int ks[3] = {k == 1 ? nz : k - 1, k, k == nz ? 1 : k + 1};
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            const int row = (ks[a] - 1) * ny + (js[b] - 1);
-            R.x[a][b] = row * (nx + 1);
-            R.c[a][b] = row * nx;
-        }
+    for (int a = 0; a < 3; ++a) {
+        R.kx[a] = (ks[a] - 1) * ny * (nx + 1);
+        R.jx[a] = (js[a] - 1) * (nx + 1);
+        R.kc[a] = (ks[a] - 1) * ny * nx;
+        R.jc[a] = (js[a] - 1) * nx;
+    }
     return R;
 }
 
@@ -302,10 +366,10 @@ struct AdjPop {
     {
         const T tyo = p == 0 ? T(1) : P.ty_om, tym = P.ty_m, tzo = p == 0 ? T(1) : P.tz_om, tzm = P.tz_m;
         const T *base = LX + (long long)p * nfx;
-        T s = (ay ? tyo : T(1)) * (az ? tzo : T(1)) * base[R.x[1][1] + I];
-        if (ay) s += tym * (az ? tzo : T(1)) * base[R.x[1][1 + ay] + I];
-        if (az) s += (ay ? tyo : T(1)) * tzm * base[R.x[1 + az][1] + I];
-        if (ay && az) s += tym * tzm * base[R.x[1 + az][1 + ay] + I];
+        T s = (ay ? tyo : T(1)) * (az ? tzo : T(1)) * base[R.x(1, 1) + I];
+        if (ay) s += tym * (az ? tzo : T(1)) * base[R.x(1, 1 + ay) + I];
+        if (az) s += (ay ? tyo : T(1)) * tzm * base[R.x(1 + az, 1) + I];
+        if (ay && az) s += tym * tzm * base[R.x(1 + az, 1 + ay) + I];
         return s;
     }
     // x weight of face I: anchor (which = 0) or other column (which = 1)
@@ -323,19 +387,19 @@ struct AdjPop {
         {
             const T *base = LY + (long long)p * nfc;
             const T yo = p == 0 ? T(0.5) : P.yn_om[p], ym = p == 0 ? T(0.5) : P.yn_m[p];
-            sy = yo * base[R.c[1][1] + c] + ym * base[R.c[1][0] + c];
+            sy = yo * base[R.c(1, 1) + c] + ym * base[R.c(1, 0) + c];
             if (az) {
                 sy = tzo * sy;
-                sy += tzm * (yo * base[R.c[1 + az][1] + c] + ym * base[R.c[1 + az][0] + c]);
+                sy += tzm * (yo * base[R.c(1 + az, 1) + c] + ym * base[R.c(1 + az, 0) + c]);
             }
         }
         {
             const T *base = LZ + (long long)p * nfc;
             const T zo = p == 0 ? T(0.5) : P.zn_om[p], zm = p == 0 ? T(0.5) : P.zn_m[p];
-            sz = zo * base[R.c[1][1] + c] + zm * base[R.c[0][1] + c];
+            sz = zo * base[R.c(1, 1) + c] + zm * base[R.c(0, 1) + c];
             if (ay) {
                 sz = tyo * sz;
-                sz += tym * (zo * base[R.c[1][1 + ay] + c] + zm * base[R.c[0][1 + ay] + c]);
+                sz += tym * (zo * base[R.c(1, 1 + ay) + c] + zm * base[R.c(0, 1 + ay) + c]);
             }
         }
         return sy + sz;
@@ -398,12 +462,15 @@ __global__ void __launch_bounds__(128) adj_ghost_kernel(const T *__restrict__ LX
                          GH, o);
 }
 
-template <class T, class S, int p>
-__device__ __forceinline__ void adj_mu_pop(T mu[NPOP], const T *__restrict__ LX, const T *__restrict__ LY,
-                                           const T *__restrict__ LZ, const T *__restrict__ GH,
-                                           const S *__restrict__ lam_next, const StepParams<T, S> &P,
-                                           const AdjRows &R, int i, long long c, long long o, int Ix2,
-                                           bool x2_anchor, long long nfx, long long nfc)
+// Transposed interpolation stencil of every population at one cell (the
+// part of mu that comes from the faces), stored population by population:
+// MU[p * ncell + cell], cell = ((k-1)*ny + (j-1))*nx + (i-1).
+template <class T, class S, int p, int pend>
+__device__ __forceinline__ void adj_stencil_pops(const T *__restrict__ LX, const T *__restrict__ LY,
+                                                 const T *__restrict__ LZ, const T *__restrict__ GH,
+                                                 const StepParams<T, S> &P, const AdjRows &R, int i, long long o,
+                                                 int Ix2, bool x2_anchor, long long nfx, long long nfc,
+                                                 T *__restrict__ MU, long long cc)
 {
     constexpr int ax = cx(p);
     // second column of the y / z faces: i + cx (periodic image, or none past a wall)
@@ -414,7 +481,7 @@ __device__ __forceinline__ void adj_mu_pop(T mu[NPOP], const T *__restrict__ LX,
         else if (i2 < 1 || i2 > P.nx) i2 = 0;
     }
     const AdjPop<p, T, S> A{LX, LY, LZ, P, R, nfx, nfc};
-    T m = T(4.0 / 3.0) * T(lam_next[p * P.ps + c]) + A.interior(i, Ix2, x2_anchor, i2);
+    T m = A.interior(i, Ix2, x2_anchor, i2);
     if (!P.periodic_x && (i <= 2 || i >= P.nx - 1)) {
         // wall ghosts: g0 = q0 fb1 + (1-q0) fb2, g_{nx+1} = q1 fb_nx + (1-q1) fb_{nx-1}
         const long long nyz = (long long)P.ny * P.nz;
@@ -424,19 +491,36 @@ __device__ __forceinline__ void adj_mu_pop(T mu[NPOP], const T *__restrict__ LX,
         if (i == P.nx) m += P.q1 * g1;
         if (i == P.nx - 1) m += (T(1) - P.q1) * g1;
     }
-    mu[p] = m;
+    MU[(long long)p * nfc + cc] = m;
+    if constexpr (p + 1 < pend)
+        adj_stencil_pops<T, S, p + 1, pend>(LX, LY, LZ, GH, P, R, i, o, Ix2, x2_anchor, nfx, nfc, MU, cc);
 }
 
-template <class T, class S, int p = 0>
-__device__ __forceinline__ void adj_mu_all(T mu[NPOP], const T *__restrict__ LX, const T *__restrict__ LY,
-                                           const T *__restrict__ LZ, const T *__restrict__ GH,
-                                           const S *__restrict__ lam_next, const StepParams<T, S> &P,
-                                           const AdjRows &R, int i, long long c, long long o, int Ix2,
-                                           bool x2_anchor, long long nfx, long long nfc)
+// Transposed stencil pass of the gather, split from the stage-(a) transpose so
+// that it runs with few registers and many warps in flight (it is bound by
+// the latency of its ~250 scattered loads per cell).  The populations are
+// split into four groups, one per block (blockIdx.z = plane * 4 + group), so
+// that each thread carries a quarter of the loads.
+template <class T, class S>
+__global__ void __launch_bounds__(128, 12) adj_stencil_kernel(const T *__restrict__ LX, const T *__restrict__ LY,
+                                                             const T *__restrict__ LZ, const T *__restrict__ GH,
+                                                             T *__restrict__ MU, const StepParams<T, S> P)
 {
-    adj_mu_pop<T, S, p>(mu, LX, LY, LZ, GH, lam_next, P, R, i, c, o, Ix2, x2_anchor, nfx, nfc);
-    if constexpr (p + 1 < NPOP)
-        adj_mu_all<T, S, p + 1>(mu, LX, LY, LZ, GH, lam_next, P, R, i, c, o, Ix2, x2_anchor, nfx, nfc);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y + 1, k = blockIdx.z / 4 + 1, grp = blockIdx.z % 4;
+    if (i > P.nx) return;
+    const AdjRows R = adj_rows(j, k, P.nx, P.ny, P.nz);
+    const long long nfx = adj_nface(0, P.nx, P.ny, P.nz), nfc = adj_nface(1, P.nx, P.ny, P.nz);
+    // second x face holding column i: face i-1 ("other" column), face 0 (anchor) at a wall,
+    // face nx ("other") for i = 1 when periodic
+    const bool wall1 = !P.periodic_x && i == 1;
+    const int Ix2 = i == 1 ? (P.periodic_x ? P.nx : 0) : i - 1;
+    const long long o = (long long)(k - 1) * P.ny + (j - 1);
+    const long long cc = adj_cell(i, j, k, P.nx, P.ny);
+    if (grp == 0) adj_stencil_pops<T, S, 0, 5>(LX, LY, LZ, GH, P, R, i, o, Ix2, wall1, nfx, nfc, MU, cc);
+    else if (grp == 1) adj_stencil_pops<T, S, 5, 10>(LX, LY, LZ, GH, P, R, i, o, Ix2, wall1, nfx, nfc, MU, cc);
+    else if (grp == 2) adj_stencil_pops<T, S, 10, 15>(LX, LY, LZ, GH, P, R, i, o, Ix2, wall1, nfx, nfc, MU, cc);
+    else adj_stencil_pops<T, S, 15, NPOP>(LX, LY, LZ, GH, P, R, i, o, Ix2, wall1, nfx, nfc, MU, cc);
 }
 
 // mu = 4/3 lam' + (G^T L^T lamv); lam = (dA/df)^T mu - 1/3 lam'.
@@ -455,7 +539,7 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
                                                          const T *__restrict__ LZ, S *__restrict__ lam_out,
                                                          const T *__restrict__ LFX, const T *__restrict__ LFY,
                                                          const T *__restrict__ LFZ, double *__restrict__ dphi,
-                                                         const T *__restrict__ GH, const StepParams<T, S> P)
+                                                         const T *__restrict__ MU, const StepParams<T, S> P)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int j = blockIdx.y + 1, k = blockIdx.z + 1;
@@ -463,14 +547,9 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
     const long long c = ((long long)(k - 1) * P.ny + (j - 1)) * P.pitch + (i - 1);
     T mu[NPOP];
     {
-        const AdjRows R = adj_rows(j, k, P.nx, P.ny, P.nz);
-        const long long nfx = adj_nface(0, P.nx, P.ny, P.nz), nfc = adj_nface(1, P.nx, P.ny, P.nz);
-        // second x face holding column i: face i-1 ("other" column), face 0 (anchor) at a wall,
-        // face nx ("other") for i = 1 when periodic
-        const bool wall1 = !P.periodic_x && i == 1;
-        const int Ix2 = i == 1 ? (P.periodic_x ? P.nx : 0) : i - 1;
-        const long long o = (long long)(k - 1) * P.ny + (j - 1);
-        adj_mu_all<T, S>(mu, LX, LY, LZ, GH, lam_next, P, R, i, c, o, Ix2, wall1, nfx, nfc);
+        const long long nfc = adj_nface(1, P.nx, P.ny, P.nz), cc = adj_cell(i, j, k, P.nx, P.ny);
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) mu[p] = T(4.0 / 3.0) * T(lam_next[p * P.ps + c]) + MU[p * nfc + cc];
     }
     // stage (a) transpose at this cell
     T v[NPOP];
@@ -478,7 +557,7 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
     for (int p = 0; p < NPOP; ++p) v[p] = T(f[p * P.ps + c]);
     T r, jx, jy, jz;
     moments(v, r, jx, jy, jz);
-    const T inv = T(1) / r;
+    const T inv = recip(r);
     const T u0 = jx * inv, v0 = jy * inv, w0 = jz * inv;
     T Fx, Fy, Fz;
     cell_force(P, i - 1, j - 1, k - 1, Fx, Fy, Fz);
@@ -494,6 +573,9 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
     T fe[NPOP];
     feq_all(r, u, vv, w, fe);
     AdjJac<T> Jc = {T(0), {T(0), T(0), T(0)}};
+    // with a field: L0 = sum mu_p feq_p and L1 = sum mu_p c_{a,p} feq_p along the field axis a
+    const int fax = P.ffaxis;
+    T L0 = T(0), L1 = T(0);
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
         T K = P.Kb[p];
@@ -505,6 +587,12 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
             K = P.bw0x3 * cf;
         }
         adj_accum(Jc, p, mu[p], r, u, vv, w, B + K, fe[p], P.bw0x3, Fc);
+        if (P.ffield) {
+            const T mf = mu[p] * fe[p];
+            L0 += mf;
+            const int ca = fax == 0 ? cx(p) : (fax == 1 ? cy(p) : cz(p));
+            if (ca) L1 += ca > 0 ? mf : -mf;
+        }
     }
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
@@ -513,30 +601,25 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
         lam_out[p * P.ps + c] = S(out);
     }
     if (dphi && P.ffield) {
-        // stage (a): d fb_p / dF_a = 3 bw0 (c_ap - u_a - hdt F_a) feq_p + coef_p hdt d feq_p / d u_a
-        const int ax = P.ffaxis;
-        const T ua = ax == 0 ? u : (ax == 1 ? vv : w);
-        const T Fa = Fc[ax];
-        T Sc = T(0), Gq = T(0);
-#pragma unroll
-        for (int p = 0; p < NPOP; ++p) {
-            const T ca = T(ax == 0 ? cx(p) : (ax == 1 ? cy(p) : cz(p)));
-            const T cfp = T(cx(p)) * Fx + T(cy(p)) * Fy + T(cz(p)) * Fz;
-            const T coef = B + P.bw0x3 * cfp;
-            const T cu = T(cx(p)) * u + T(cy(p)) * vv + T(cz(p)) * w;
-            Sc += mu[p] * (ca - ua - P.hdt * Fa) * fe[p];
-            Gq += mu[p] * coef * weight<T>(p) * r * (T(3) * ca + T(9) * cu * ca - T(3) * ua);
-        }
-        double g = double(P.bw0x3 * Sc + P.hdt * Gq);
+        // stage (a): d fb_p / dF_a = 3 bw0 (c_ap - u_a - hdt F_a) feq_p + coef_p hdt d feq_p / d u_a;
+        // summed with mu: Sc = L1 - (u_a + hdt F_a) L0 and, since Jc.G[a] holds the second
+        // sum minus 3 bw0 F_a L0, Gq = Jc.G[a] + 3 bw0 F_a L0
+        const T ua = fax == 0 ? u : (fax == 1 ? vv : w);
+        const T Fa = fax == 0 ? Fx : (fax == 1 ? Fy : Fz);
+        const T Ga = fax == 0 ? Jc.G[0] : (fax == 1 ? Jc.G[1] : Jc.G[2]);
+        const T Sc = L1 - (ua + P.hdt * Fa) * L0;
+        const T Gq = Ga + P.bw0x3 * Fa * L0;
+        // this step's contribution in the arithmetic type, accumulated over steps in FP64
+        T g = P.bw0x3 * Sc + P.hdt * Gq;
         // faces: the field enters each face through the mean over its two cells
         const int nx = P.nx, ny = P.ny, nz = P.nz;
         const int Il = P.periodic_x && i == 1 ? nx : i - 1;
-        g += double(xface_share(P, Il, i) * LFX[adj_xface(Il, j, k, nx, ny)]);
-        g += double(xface_share(P, i, i) * LFX[adj_xface(i, j, k, nx, ny)]);
+        g += xface_share(P, Il, i) * LFX[adj_xface(Il, j, k, nx, ny)];
+        g += xface_share(P, i, i) * LFX[adj_xface(i, j, k, nx, ny)];
         const int jl = j == 1 ? ny : j - 1, kl = k == 1 ? nz : k - 1;
-        g += 0.5 * double(LFY[adj_cell(i, jl, k, nx, ny)]) + 0.5 * double(LFY[adj_cell(i, j, k, nx, ny)]);
-        g += 0.5 * double(LFZ[adj_cell(i, j, kl, nx, ny)]) + 0.5 * double(LFZ[adj_cell(i, j, k, nx, ny)]);
-        dphi[adj_cell(i, j, k, nx, ny)] += g;
+        g += T(0.5) * (LFY[adj_cell(i, jl, k, nx, ny)] + LFY[adj_cell(i, j, k, nx, ny)]);
+        g += T(0.5) * (LFZ[adj_cell(i, j, kl, nx, ny)] + LFZ[adj_cell(i, j, k, nx, ny)]);
+        dphi[adj_cell(i, j, k, nx, ny)] += double(g);
     }
 }
 

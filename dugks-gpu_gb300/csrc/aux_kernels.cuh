@@ -86,33 +86,49 @@ __global__ void stats_accumulate_kernel(const double *__restrict__ total, int nx
 // Conserved moments: block partial sums of (rho, jx, jy, jz) over cells.
 // Block b owns rows (j,k) = b, b+gridDim.x, ...; threads stride x (coalesced);
 // fixed assignment and a fixed-order tree make the sums reproducible.
+// Warp-shuffle sum of a double over the 32 lanes (fixed order: deterministic).
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Mass and momentum partial sums, one per block (deterministic order): each
+// thread sums the moments of its cells (per cell in the arithmetic type, over
+// cells in FP64), warps reduce with shuffles, warp 0 combines the warps.
 template <class T, class S>
 __global__ void __launch_bounds__(256) moments_partials_kernel(const S *__restrict__ f, const StepParams<T, S> P,
                                                                double *__restrict__ partial)
 {
-    __shared__ double red[4][256];
-    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    __shared__ double red[8][4];
+    double a[4] = {0, 0, 0, 0};
     const int rows = P.ny * P.nz;
     for (int row = blockIdx.x; row < rows; row += gridDim.x) {
         for (int i = threadIdx.x; i < P.nx; i += blockDim.x) {
             const long long c = (long long)row * P.pitch + i;
-            double v[NPOP];
+            T v[NPOP];
 #pragma unroll
-            for (int p = 0; p < NPOP; ++p) v[p] = double(P.codec.load_nc(f, p * P.ps + c, p));
-            double r, jx, jy, jz;
+            for (int p = 0; p < NPOP; ++p) v[p] = P.codec.load_nc(f, p * P.ps + c, p);
+            T r, jx, jy, jz;
             moments(v, r, jx, jy, jz);
-            a0 += r; a1 += jx; a2 += jy; a3 += jz;
+            a[0] += double(r); a[1] += double(jx); a[2] += double(jy); a[3] += double(jz);
         }
     }
-    red[0][threadIdx.x] = a0; red[1][threadIdx.x] = a1; red[2][threadIdx.x] = a2; red[3][threadIdx.x] = a3;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s)
-            for (int m = 0; m < 4; ++m) red[m][threadIdx.x] += red[m][threadIdx.x + s];
-        __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        const double s = warp_sum(a[m]);
+        if (lane == 0) red[warp][m] = s;
     }
-    if (threadIdx.x == 0)
-        for (int m = 0; m < 4; ++m) partial[blockIdx.x * 4 + m] = red[m][0];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+            const double s = warp_sum(lane < 8 ? red[lane][m] : 0.0);
+            if (lane == 0) partial[blockIdx.x * 4 + m] = s;
+        }
+    }
 }
 
 }  // namespace dg

@@ -119,7 +119,8 @@ __device__ __forceinline__ void moments(const T v[NPOP], T &r, T &jx, T &jy, T &
 
 // 1/r: FP64 from a single-precision seed and two Newton steps (error at the
 // rounding level), cheaper than the full-precision divide on the FP64 pipe;
-// the native reciprocal for FP32.
+// the correctly rounded FP32 reciprocal (same result as 1.0f / r, without the
+// division's multi-instruction sequence) for FP32.
 __device__ __forceinline__ double recip(double r)
 {
     double x = double(__frcp_rn(float(r)));
@@ -128,7 +129,7 @@ __device__ __forceinline__ double recip(double r)
     e = fma(-r, x, 1.0);
     return fma(x, e, x);
 }
-__device__ __forceinline__ float recip(float r) { return 1.0f / r; }
+__device__ __forceinline__ float recip(float r) { return __frcp_rn(r); }
 
 // All 19 equilibria for density r and velocity (u, v, w).
 template <class T>
@@ -147,6 +148,31 @@ __device__ __forceinline__ void feq_all(T r, T u, T v, T w, T fe[NPOP])
     feq_pair(w3 - u3, base, wr2, fe[12], fe[13]);
     feq_pair(v3 + w3, base, wr2, fe[15], fe[18]);
     feq_pair(w3 - v3, base, wr2, fe[16], fe[17]);
+}
+
+// The equilibria of the 10 populations that cross a face normal to AX (the
+// others are left unset).
+template <class T, int AX>
+__device__ __forceinline__ void feq_face(T r, T u, T v, T w, T fe[NPOP])
+{
+    const T u3 = T(3) * u, v3 = T(3) * v, w3 = T(3) * w;
+    const T base = fma(T(-1.5), fma(u, u, fma(v, v, w * w)), T(1));
+    const T wr1 = weight<T>(1) * r, wr2 = weight<T>(7) * r;
+    if (AX == 0) feq_pair(u3, base, wr1, fe[1], fe[2]);
+    else if (AX == 1) feq_pair(v3, base, wr1, fe[3], fe[4]);
+    else feq_pair(w3, base, wr1, fe[5], fe[6]);
+    if (AX != 2) {
+        feq_pair(u3 + v3, base, wr2, fe[7], fe[10]);
+        feq_pair(v3 - u3, base, wr2, fe[8], fe[9]);
+    }
+    if (AX != 1) {
+        feq_pair(u3 + w3, base, wr2, fe[11], fe[14]);
+        feq_pair(w3 - u3, base, wr2, fe[12], fe[13]);
+    }
+    if (AX != 0) {
+        feq_pair(v3 + w3, base, wr2, fe[15], fe[18]);
+        feq_pair(w3 - v3, base, wr2, fe[16], fe[17]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -206,6 +232,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
 
     T fe[NPOP];
     feq_all(r, u, vv, w, fe);
+    const unsigned hc = P.codec.cell_hash(cb);
 
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
@@ -218,7 +245,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
             K = P.bw0x3 * cf;
         }
         const T out = fma(B + K, fe[p], P.bw1 * v[p]);
-        P.codec.store(fb, p * P.ps_b + cb, p, out);
+        P.codec.store_h(fb, p * P.ps_b + cb, p, out, hc);
     }
 }
 
@@ -494,7 +521,9 @@ __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[N
     T Ff[3] = {P.F[0], P.F[1], P.F[2]};
     if (FF) {
         // face force with the field: shift (hdt/2) F_face
-        Ff[P.ffaxis] += fadd;
+        Ff[0] += P.ffaxis == 0 ? fadd : T(0);  // selects: no dynamically indexed local array
+        Ff[1] += P.ffaxis == 1 ? fadd : T(0);
+        Ff[2] += P.ffaxis == 2 ? fadd : T(0);
         const T hh = T(0.5) * P.hdt;
         u = fma(hh, Ff[0], u);
         vv = fma(hh, Ff[1], vv);
@@ -646,6 +675,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict_
             }
             if (cell) {
                 const long long c = ((long long)(k - 1) * ny + (gj - 1)) * P.pitch + (gi - 1);
+                const unsigned hc = P.codec.cell_hash(c);
                 const long long cb = R.rb(gj, k) + gi;
                 const T cxg = __ldg(P.cxuf + gi);
                 const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
@@ -665,7 +695,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict_
                         const int s = flux_slot(2, p);
                         r = fma(cz(p) > 0 ? -P.czuf : P.czuf, fzu[s] - fzd[s], r);
                     }
-                    P.codec.store(f_out, p * P.ps + c, p, r);
+                    P.codec.store_h(f_out, p * P.ps + c, p, r, hc);
                 }
             }
 #pragma unroll
@@ -826,6 +856,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
             }
             if (cell) {
                 const long long c = ((long long)(k - 1) * ny + (gj - 1)) * P.pitch + (gi - 1);
+                const unsigned hc = P.codec.cell_hash(c);
                 const int cb = R.rb(gj, k) + gi;
                 const T cxg = __ldg(P.cxuf + gi);
                 const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
@@ -844,7 +875,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
                         const int s = flux_slot(2, p);
                         r = fma(cz(p) > 0 ? -P.czuf : P.czuf, fzu[s] - fzd[s], r);
                     }
-                    P.codec.store(f_out, p * P.ps + c, p, r);
+                    P.codec.store_h(f_out, p * P.ps + c, p, r, hc);
                 }
             }
 #pragma unroll

@@ -138,6 +138,7 @@ struct dg_ctx {
     double *acc = nullptr;        // running sums of the per-x statistics (dg_stats_accumulate)
     int *dev_err = nullptr;       // device error flag written by the kernels (TMA wait time-outs)
     CUtensorMap tmap;             // f-bar-plus tensor map of the TMA flux kernel (64-byte aligned type)
+    CUtensorMap tmap_adj;         // the same array with the adjoint face kernel's box
     bool have_tmap = false;
     long long acc_count = 0;
     bool macro_valid = false;
@@ -627,11 +628,14 @@ int adjoint_form(dg_ctx *h, int istep, const void *f_n, const void *lam_next, vo
     using K = Kern<T, S>;
     if (!std::is_same<T, S>::value) return h->fail(DG_ERR_UNSUPPORTED, "the adjoint exists for the fp64 and fp32 forms");
     if (!h->adj) {
-        // 19 adjoint values and one dJ/dF (force-field face term) per face, then the
-        // wall-ghost sums (2 * 19 per row and plane)
+        // 19 adjoint values and one dJ/dF (force-field face term) per face, the
+        // wall-ghost sums (2 * 19 per row and plane) and the transposed-stencil
+        // sums (19 per cell)
         const long long n = adj_nface(0, h->nx, h->ny, h->nz) + 2 * adj_nface(1, h->nx, h->ny, h->nz);
         const long long ng = 2LL * NPOP * h->ny * h->nz;
-        CK(cudaMalloc(&h->adj, (size_t(n) * (NPOP + 1) + size_t(ng)) * sizeof(T)), "cudaMalloc (adjoint scratch)");
+        const long long nm = (long long)NPOP * h->ncell();
+        CK(cudaMalloc(&h->adj, (size_t(n) * (NPOP + 1) + size_t(ng) + size_t(nm)) * sizeof(T)),
+           "cudaMalloc (adjoint scratch)");
     }
     if (h->ffield && !h->dphi) {
         CK(cudaMalloc(&h->dphi, h->ncell() * sizeof(double)), "cudaMalloc (field gradient)");
@@ -639,7 +643,7 @@ int adjoint_form(dg_ctx *h, int istep, const void *f_n, const void *lam_next, vo
     }
     CK(K::adjoint(static_cast<const S *>(f_n), static_cast<S *>(h->fb), static_cast<const S *>(lam_next),
                   static_cast<S *>(lam_out), static_cast<T *>(h->adj), params_for<T, S>(h, istep),
-                  h->ffield ? h->dphi : nullptr, h->stream),
+                  h->ffield ? h->dphi : nullptr, h->have_tmap ? &h->tmap_adj : nullptr, h->stream),
        "adjoint launch");
     h->macro_valid = false;
     return DG_OK;
@@ -681,7 +685,9 @@ int make_tmap_form(dg_ctx *h)
 {
     using K = Kern<T, S>;
     if (!K::uses_tma()) return DG_OK;
-    const int r = K::make_tmap(static_cast<const S *>(h->fb), h->nx, h->ny, h->nz, h->pitch_b, h->ps_b, &h->tmap);
+    const S *fb = static_cast<const S *>(h->fb);
+    int r = K::make_tmap(fb, h->nx, h->ny, h->nz, h->pitch_b, h->ps_b, TileCfg<T, S>::W + 1, &h->tmap);
+    if (!r) r = K::make_tmap(fb, h->nx, h->ny, h->nz, h->pitch_b, h->ps_b, AdjCfg<T, S>::W + 2, &h->tmap_adj);
     if (r) return h->fail(DG_ERR_CUDA, "cuTensorMapEncodeTiled failed for the f-bar-plus tensor map (" + std::to_string(r) + ")");
     h->have_tmap = true;
     return DG_OK;

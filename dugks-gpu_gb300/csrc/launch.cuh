@@ -31,6 +31,13 @@ struct TileCfg<double, double> {
     static constexpr bool TMA = false;
 };
 
+// tile of the fused adjoint face kernel (TMA forms): W rows of 32 cells, box W+2 rows
+template <class T, class S>
+struct AdjCfg {
+    static constexpr int W = 6;       // 4 x 21.9 KB planes (FP32), two CTAs per SM
+    static constexpr int MINB = 2;
+};
+
 template <class T, class S>
 struct Kern {
     // stage (a) and the x ghost columns of f-bar-plus
@@ -41,8 +48,11 @@ struct Kern {
     static cudaError_t flux(const S *fb, const S *f_in, S *f_out, const StepParams<T, S> &P, int recon,
                             const CUtensorMap *tmap, cudaStream_t st);
     static bool uses_tma() { return TileCfg<T, S>::TMA; }
-    // 4-D tensor map (x, y, z, population) over the ghosted f-bar-plus array
-    static int make_tmap(const S *fb, int nx, int ny, int nz, int pitch_b, long long ps_b, CUtensorMap *out);
+    // 4-D tensor map (x, y, z, population) over the ghosted f-bar-plus array,
+    // box of TmaTile::BXT columns x box_rows rows x 1 plane x 19 populations
+    // (forward flux kernel: TileCfg::W + 1 rows; adjoint faces: AdjCfg::W + 2)
+    static int make_tmap(const S *fb, int nx, int ny, int nz, int pitch_b, long long ps_b, int box_rows,
+                         CUtensorMap *out);
     static cudaError_t macro(const S *f, const StepParams<T, S> &P, double hdt, const double F[3], double *rho,
                              double *ux, double *uy, double *uz, cudaStream_t st);
     static cudaError_t aos_to_soa(const double *src, S *dst, const StepParams<T, S> &P, cudaStream_t st);
@@ -54,9 +64,11 @@ struct Kern {
     // Adjoint of one step (adjoint_kernels.cuh): recomputes f-bar-plus of f_n into fb,
     // per-face adjoints into lamv (T-typed scratch, adj_nface(0)+2*adj_nface(1) faces x 19),
     // then lam_out = (dS/df)^T lam_next.  FP64 and FP32 forms only.
-    // dphi (optional, FP64, dump order [k][j][i]): += dJ/dphi of this step when a force field is set
+    // dphi (optional, FP64, dump order [k][j][i]): += dJ/dphi of this step when a force field is set;
+    // tmap_adj: f-bar-plus tensor map with AdjCfg::W + 2 rows (TMA forms)
     static cudaError_t adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_out, T *lamv,
-                               const StepParams<T, S> &P, double *dphi, cudaStream_t st);
+                               const StepParams<T, S> &P, double *dphi, const CUtensorMap *tmap_adj,
+                               cudaStream_t st);
     static int flux_kchunk(const StepParams<T, S> &P);
 };
 

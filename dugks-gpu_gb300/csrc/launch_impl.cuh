@@ -18,36 +18,23 @@ cudaError_t Kern<T, S>::fbar(const S *f, S *fb, const StepParams<T, S> &P, cudaS
     return cudaGetLastError();
 }
 
-template <class T, class S>
-int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
+// Chunk length along z for a grid of `cols` CTA columns and `slots` resident
+// CTAs: every chunk re-evaluates one bottom z face (1/(3k) of the face work
+// for k planes) and refills the plane pipeline (about half a plane), and the
+// last wave of CTAs may be partly empty; maximise
+// (useful waves / launched waves) * (1 - 1/(3k)) * (1 - 1/(2k)) over chunk
+// lengths k >= 4, keeping at least two waves where the grid allows it so that
+// the scheduler can even out tiles of unequal work (partial rows).
+static int choose_kchunk(int nz, long long cols, long long slots)
 {
-    constexpr int W = TileCfg<T, S>::W, MB = TileCfg<T, S>::MINB;
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int occ = 1;
-    if constexpr (TileCfg<T, S>::TMA)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_tma_kernel<T, S, W, 0, MB, false>, 32 * W,
-                                                      flux_tma_smem_bytes<T, S, W>());
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0, MB, false>, 32 * W, 0);
-    occ = std::max(occ, 1);
-    const long long cols = (long long)((P.nx + 31) / 32) * ((P.ny + W - 2) / (W - 1));
-    const long long slots = (long long)sms * occ;
-    // Pick the z chunking: every chunk re-evaluates one bottom z face (1/(3k) of
-    // the face work for k planes) and refills the plane pipeline (about half a
-    // plane), and the last wave of CTAs may be partly empty; maximise
-    // (useful waves / launched waves) * (1 - 1/(3k)) * (1 - 1/(2k)) over chunk
-    // lengths k >= 4, keeping at least two waves where the grid allows it so
-    // that the scheduler can even out tiles of unequal work (partial rows).
-    const int kmin = std::min(P.nz, 4);
-    const long long max_chunks = (P.nz + kmin - 1) / kmin;
+    const int kmin = std::min(nz, 4);
+    const long long max_chunks = (nz + kmin - 1) / kmin;
     const double min_waves = std::min(2.0, double(cols * max_chunks) / double(slots));
-    int best_k = P.nz;
+    int best_k = nz;
     double best = -1.0;
-    for (int k = kmin; k <= P.nz; ++k) {
-        const long long nch = (P.nz + k - 1) / k;
-        if (k > kmin && (P.nz + k - 2) / (k - 1) == nch) continue;  // same chunk count as k-1
+    for (int k = kmin; k <= nz; ++k) {
+        const long long nch = (nz + k - 1) / k;
+        if (k > kmin && (nz + k - 2) / (k - 1) == nch) continue;  // same chunk count as k-1
         const double waves = double(cols * nch) / double(slots);
         if (waves < min_waves - 1e-9) break;  // fewer chunks only lower the wave count further
         const double fill = waves / std::ceil(waves);
@@ -58,6 +45,30 @@ int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
         }
     }
     return best_k;
+}
+
+static int device_sms()
+{
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms;
+}
+
+template <class T, class S>
+int Kern<T, S>::flux_kchunk(const StepParams<T, S> &P)
+{
+    constexpr int W = TileCfg<T, S>::W, MB = TileCfg<T, S>::MINB;
+    const int sms = device_sms();
+    int occ = 1;
+    if constexpr (TileCfg<T, S>::TMA)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_tma_kernel<T, S, W, 0, MB, false>, 32 * W,
+                                                      flux_tma_smem_bytes<T, S, W>());
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, flux_kernel<T, S, W, 0, MB, false>, 32 * W, 0);
+    occ = std::max(occ, 1);
+    const long long cols = (long long)((P.nx + 31) / 32) * ((P.ny + W - 2) / (W - 1));
+    return choose_kchunk(P.nz, cols, (long long)sms * occ);
 }
 
 // one launch of the flux kernel variant <RECON, FF>
@@ -147,7 +158,8 @@ cudaError_t Kern<T, S>::moments_partials(const S *f, const StepParams<T, S> &P, 
 
 template <class T, class S>
 cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_out, T *lamv,
-                                const StepParams<T, S> &P, double *dphi, cudaStream_t st)
+                                const StepParams<T, S> &P, double *dphi, const CUtensorMap *tmap_adj,
+                                cudaStream_t st)
 {
     if constexpr (!std::is_same<T, S>::value) {
         return cudaErrorNotSupported;
@@ -157,9 +169,31 @@ cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_o
         const long long nfx = adj_nface(0, P.nx, P.ny, P.nz), nfc = adj_nface(1, P.nx, P.ny, P.nz);
         T *LX = lamv, *LY = lamv + NPOP * nfx, *LZ = LY + NPOP * nfc;
         T *LFX = LZ + NPOP * nfc, *LFY = LFX + nfx, *LFZ = LFY + nfc;  // per-face dJ/dF (force field)
-        adj_face_kernel<T, S, 0><<<unsigned((nfx + 127) / 128), 128, 0, st>>>(fb, lam_next, LX, LFX, P);
-        adj_face_kernel<T, S, 1><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LY, LFY, P);
-        adj_face_kernel<T, S, 2><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LZ, LFZ, P);
+        if constexpr (TileCfg<T, S>::TMA) {
+            // +x, +y, +z faces of every cell from the TMA-staged tile; x faces I = 0 apart
+            if (!tmap_adj) return cudaErrorInvalidValue;
+            constexpr int W = AdjCfg<T, S>::W, MB = AdjCfg<T, S>::MINB;
+            auto kern = adj_faces_tma_kernel<T, S, W, MB>;
+            const size_t smem = adj_faces_tma_smem_bytes<T, S, W>();
+            static bool attr_set = false;
+            if (!attr_set) {
+                e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+                if (e != cudaSuccess) return e;
+                attr_set = true;
+            }
+            int occ = 1;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 32 * W, smem);
+            const long long cols = (long long)((P.nx + 31) / 32) * ((P.ny + W - 1) / W);
+            const int kchunk = choose_kchunk(P.nz, cols, (long long)device_sms() * std::max(occ, 1));
+            dim3 grid((P.nx + 31) / 32, (P.ny + W - 1) / W, (P.nz + kchunk - 1) / kchunk);
+            kern<<<grid, dim3(32, W), smem, st>>>(*tmap_adj, lam_next, LX, LY, LZ, LFX, LFY, LFZ, P, kchunk);
+            const long long n0 = (long long)P.ny * P.nz;
+            adj_face_kernel<T, S, 0><<<unsigned((n0 + 127) / 128), 128, 0, st>>>(fb, lam_next, LX, LFX, P, 1);
+        } else {
+            adj_face_kernel<T, S, 0><<<unsigned((nfx + 127) / 128), 128, 0, st>>>(fb, lam_next, LX, LFX, P, 0);
+            adj_face_kernel<T, S, 1><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LY, LFY, P, 0);
+            adj_face_kernel<T, S, 2><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LZ, LFZ, P, 0);
+        }
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         T *GH = LFZ + nfc;  // wall-ghost sums, 2 * 19 * ny * nz
@@ -167,14 +201,17 @@ cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_o
             const long long ng = 2LL * P.ny * P.nz;
             adj_ghost_kernel<T, S><<<unsigned((ng + 127) / 128), 128, 0, st>>>(LX, LY, LZ, GH, P);
         }
+        T *MU = GH + 2LL * NPOP * P.ny * P.nz;  // transposed-stencil sums, 19 * nx * ny * nz
         dim3 grid((P.nx + 127) / 128, P.ny, P.nz);
-        adj_gather_kernel<T, S><<<grid, 128, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, LFX, LFY, LFZ, dphi, GH, P);
+        adj_stencil_kernel<T, S><<<dim3(grid.x, grid.y, 4 * P.nz), 128, 0, st>>>(LX, LY, LZ, GH, MU, P);
+        adj_gather_kernel<T, S><<<grid, 128, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, LFX, LFY, LFZ, dphi, MU, P);
         return cudaGetLastError();
     }
 }
 
 template <class T, class S>
-int Kern<T, S>::make_tmap(const S *fb, int nx, int ny, int nz, int pitch_b, long long ps_b, CUtensorMap *out)
+int Kern<T, S>::make_tmap(const S *fb, int nx, int ny, int nz, int pitch_b, long long ps_b, int box_rows,
+                          CUtensorMap *out)
 {
     static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
     if (!encode) {
@@ -186,7 +223,6 @@ int Kern<T, S>::make_tmap(const S *fb, int nx, int ny, int nz, int pitch_b, long
             return -1;
         encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
-    constexpr int W = TileCfg<T, S>::W;
     const CUtensorMapDataType dt = sizeof(S) == 8   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64
                                    : sizeof(S) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                    : std::is_same<S, __half>::value ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
@@ -194,7 +230,7 @@ int Kern<T, S>::make_tmap(const S *fb, int nx, int ny, int nz, int pitch_b, long
     const cuuint64_t dims[4] = {cuuint64_t(nx + 2), cuuint64_t(ny + 2), cuuint64_t(nz + 2), cuuint64_t(NPOP)};
     const cuuint64_t strides[3] = {cuuint64_t(pitch_b) * sizeof(S), cuuint64_t(pitch_b) * (ny + 2) * sizeof(S),
                                    cuuint64_t(ps_b) * sizeof(S)};
-    const cuuint32_t box[4] = {cuuint32_t(TmaTile<S>::BXT), cuuint32_t(W + 1), 1u, cuuint32_t(NPOP)};
+    const cuuint32_t box[4] = {cuuint32_t(TmaTile<S>::BXT), cuuint32_t(box_rows), 1u, cuuint32_t(NPOP)};
     const cuuint32_t estr[4] = {1u, 1u, 1u, 1u};
     const CUresult r = encode(out, dt, 4, const_cast<S *>(fb), dims, strides, box, estr,
                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,

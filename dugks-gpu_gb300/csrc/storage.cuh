@@ -8,7 +8,10 @@
 //       sr_seed != 0: 16 hashed bits of (index, population, seed) are added
 //       below the BF16 mantissa before truncation, so the rounding error has
 //       zero mean and does not bias time averages; the seed changes every
-//       step and the result stays deterministic.
+//       step and the result stays deterministic.  The step kernels hash the
+//       cell once (cell_hash) and draw the population's bits from it with one
+//       multiply by an odd constant (store_h), a bijection of the hash, so
+//       each population's bits stay uniformly distributed.
 #pragma once
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
@@ -23,6 +26,8 @@ struct Codec {
     __device__ __forceinline__ T load_nc(const S *a, long long idx, int) const { return T(__ldg(a + idx)); }
     __device__ __forceinline__ T load_s(const S *a, int idx, int) const { return T(a[idx]); }
     __device__ __forceinline__ void store(S *a, long long idx, int, T v) const { a[idx] = S(v); }
+    __device__ __forceinline__ unsigned cell_hash(long long) const { return 0u; }
+    __device__ __forceinline__ void store_h(S *a, long long idx, int p, T v, unsigned) const { store(a, idx, p, v); }
     // undecoded reads and the decode of a value affine in them (identity here)
     __device__ __forceinline__ T raw_nc(const S *a, long long idx) const { return T(__ldg(a + idx)); }
     __device__ __forceinline__ T raw_s(const S *a, int idx) const { return T(a[idx]); }
@@ -68,6 +73,11 @@ struct Codec<float, __half> : DevCodec<__half> {
     {
         a[idx] = __float2half_rn((v - w[p]) * is[p]);
     }
+    __device__ __forceinline__ unsigned cell_hash(long long) const { return 0u; }
+    __device__ __forceinline__ void store_h(__half *a, long long idx, int p, float v, unsigned) const
+    {
+        store(a, idx, p, v);
+    }
     __device__ __forceinline__ float raw_nc(const __half *a, long long idx) const { return __half2float(__ldg(a + idx)); }
     __device__ __forceinline__ float raw_s(const __half *a, int idx) const { return __half2float(a[idx]); }
     __device__ __forceinline__ float dec(int p, float x) const { return fmaf(s[p], x, w[p]); }
@@ -97,6 +107,21 @@ struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
         const unsigned r = mix32(unsigned(idx) * 19u + unsigned(p) + sr_seed * 0x9e3779b9u);
         const unsigned u = __float_as_uint(d) + (r & 0xffffu);  // magnitude rounds up with probability = fraction
         a[idx] = __ushort_as_bfloat16((unsigned short)(u >> 16));
+    }
+    // per-cell hash of the step kernels (0: round to nearest)
+    __device__ __forceinline__ unsigned cell_hash(long long cell) const
+    {
+        return sr_seed ? (mix32(unsigned(cell) ^ sr_seed) | 1u) : 0u;
+    }
+    __device__ __forceinline__ void store_h(__nv_bfloat16 *a, long long idx, int p, float v, unsigned h) const
+    {
+        const float d = (v - w[p]) * is[p];
+        if (h == 0u) {
+            a[idx] = __float2bfloat16_rn(d);
+            return;
+        }
+        const unsigned r = (h * (0x9e3779b1u + 0x6a09e66eu * unsigned(p))) >> 16;  // odd multiplier per p
+        a[idx] = __ushort_as_bfloat16((unsigned short)((__float_as_uint(d) + r) >> 16));
     }
     __device__ __forceinline__ float raw_nc(const __nv_bfloat16 *a, long long idx) const
     {

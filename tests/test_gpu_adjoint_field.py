@@ -154,3 +154,34 @@ def test_wall_shear_fast_source_equals_autograd_source():
         out.append(torch.autograd.grad(j, [phi, t0]))
     for a, b in zip(out[0], out[1]):
         assert float((a - b).abs().max()) <= 1e-12 * float(b.abs().max())
+
+
+@pytest.mark.parametrize("case,axis", [("walls", 2), ("periodic", 0), ("stretched", 2), ("aniso", None)])
+def test_fp32_adjoint_matches_fp64(case, axis):
+    """The FP32 adjoint (TMA-staged face kernel) against the FP64 one on the same state and field."""
+    outs = []
+    for prec in ("fp64", "fp32"):
+        eng = _engine(case, prec)
+        f = seeded_state(eng.nx, eng.ny, eng.nz, seed=33)
+        lam = uniform_sym(8, f.size, 3).reshape(f.shape)
+        if axis is not None:
+            eng.set_force_field(axis, _field(eng, 11))
+            eng.field_grad(reset=True)
+        dt = torch.float64 if prec == "fp64" else torch.float32
+        ft = da.from_dump_order(eng, torch.from_numpy(f).cuda().to(dt))
+        lt = da.from_dump_order(eng, torch.from_numpy(lam).cuda().to(dt))
+        out = torch.zeros_like(lt)
+        eng.set_stream(torch.cuda.current_stream().cuda_stream)
+        eng.adjoint_step(2, ft.data_ptr(), lt.data_ptr(), out.data_ptr())
+        torch.cuda.synchronize()
+        g = eng.field_grad(reset=True) if axis is not None else None
+        outs.append((da.to_dump_order(eng, out).double().cpu().numpy(), g))
+        eng.close()
+    (a64, g64), (a32, g32) = outs
+    rel = float(np.max(np.abs(a32 - a64)) / np.max(np.abs(a64)))
+    print(f"{case}: fp32 vs fp64 adjoint rel {rel:.2e}")
+    assert rel < 1e-5
+    if axis is not None:
+        relg = float(np.max(np.abs(g32 - g64)) / np.max(np.abs(g64)))
+        print(f"{case}: fp32 vs fp64 field gradient rel {relg:.2e}")
+        assert relg < 1e-4

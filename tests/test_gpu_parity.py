@@ -57,6 +57,27 @@ def test_gradient_reconstruction_matches_oracle(case):
     assert err <= FP64_TOL
 
 
+@pytest.mark.parametrize("case", ["walls", "periodic"])
+def test_gradient_reconstruction_fp32_matches_oracle(case):
+    """recon=gradient in the FP32 form (the TMA-staged flux kernel) against the FP32 oracle."""
+    from _cases import CASES as C
+    import numpy as np
+    import pydugks
+    import pyoracle
+    from seeded import seeded_state
+    kw = dict(C[case])
+    kw["recon"] = "gradient"
+    kw["precision"] = "fp32"
+    eng = pydugks.Engine(pydugks.make_config(**kw))
+    orc = pyoracle.Oracle.from_engine_info(eng.info, recon=1, dtype=np.float32)
+    f0 = seeded_state(eng.nx, eng.ny, eng.nz, seed=3)
+    eng.set_state(f0)
+    got, want = run_both(eng, orc, f0, 1, 20)
+    err = rel_err(got, want)
+    print(f"{case} gradient fp32 20 steps: rel err {err:.3e}")
+    assert err <= FP32_TOL
+
+
 def test_step_is_deterministic():
     eng, _, f0 = make_pair("walls", "fp64")
     eng.run(1, 5)
