@@ -11,7 +11,8 @@ start (case=channel_turb, seed 0), control phi = per-cell z force field
 gradient dJ/dphi through dugks_autograd.DugksObjectiveRun with the binomial
 checkpointing schedule; the stored states are sized to <= `--snap-gb` GB.
 
-Reports, side by side: the FP32 forward step, the FP16-deviation (mixed)
+Reports, side by side: the FP32 forward step (plain, and with the control
+field set: the step the gradient differentiates), the FP16-deviation (mixed)
 forward step, the adjoint step (dg_adjoint_step alone) and the whole
 gradient (forward sweep + recomputation + adjoint) per step, and, with
 `--fd-steps`, an FP64 check of the gradient against central differences on
@@ -45,10 +46,12 @@ def _events_ms(torch, fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
-def forward_ms(torch, prec, args):
+def forward_ms(torch, prec, args, field=False):
     cfg, _ = pydugks.channel_config(nx=args.nx, ny=args.ny, nz=args.nz, precision=prec, seed=0)
     eng = pydugks.Engine(cfg)
     eng.set_stream(torch.cuda.current_stream().cuda_stream)
+    if field:  # the step the gradient differentiates: with the (zero) control field set
+        eng.set_force_field(2, np.zeros((eng.nz, eng.ny, eng.nx)))
     step = [1]
 
     def one():
@@ -91,7 +94,7 @@ def gradient_run(torch, da, args):
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     gd = g.double()
-    res = dict(J=float(J), tau_w_laminar=meta["utau"] ** 2, snaps=snaps, snap_gb=round(peak * state_bytes / 1e9, 2),
+    res = dict(J=float(J.detach()), tau_w_laminar=meta["utau"] ** 2, snaps=snaps, snap_gb=round(peak * state_bytes / 1e9, 2),
                recomputed_steps=total_adv - spine_adv,
                forward_sweep_s=round(t1 - t0, 3), backward_s=round(t2 - t1, 3),
                adjoint_ms_per_step_harness=(t2 - t1) * 1e3 / args.steps,
@@ -151,14 +154,16 @@ def main():
     import dugks_autograd as da
 
     fwd32 = forward_ms(torch, "fp32", args)
+    fwd32f = forward_ms(torch, "fp32", args, field=True)
     fwd16 = forward_ms(torch, "fp16", args)
     grad, adj_ms = gradient_run(torch, da, args)
     n = args.nx * args.ny * args.nz
     res = dict(workload=f"Re_tau=180 channel {args.nz}x{args.nx}x{args.ny} (streamwise x wall-normal tanh x spanwise)",
                steps=args.steps, cells=n,
-               forward_fp32_ms=fwd32, forward_fp16_ms=fwd16, adjoint_step_ms=adj_ms,
+               forward_fp32_ms=fwd32, forward_fp32_field_ms=fwd32f, forward_fp16_ms=fwd16, adjoint_step_ms=adj_ms,
                forward_fp32_mlups=n / fwd32 / 1e3, forward_fp16_mlups=n / fwd16 / 1e3,
-               adjoint_over_forward=adj_ms / fwd32,
+               # the adjoint (of the step with the control field) against that step, and against the plain step
+               adjoint_over_forward=adj_ms / fwd32f, adjoint_over_plain_forward=adj_ms / fwd32,
                gradient_ms_per_step=grad["adjoint_ms_per_step_harness"] + grad["forward_sweep_s"] * 1e3 / args.steps,
                **grad)
     if args.fd_steps:

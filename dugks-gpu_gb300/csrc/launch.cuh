@@ -34,7 +34,7 @@ struct TileCfg<double, double> {
 // tile of the fused adjoint face kernel (TMA forms): W rows of 32 cells, box W+2 rows
 template <class T, class S>
 struct AdjCfg {
-    static constexpr int W = 6;       // 4 x 21.9 KB planes (FP32), two CTAs per SM
+    static constexpr int W = 7;       // 4 x 24.6 KB planes (FP32), two CTAs per SM
     static constexpr int MINB = 2;
 };
 

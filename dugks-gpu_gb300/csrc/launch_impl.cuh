@@ -187,8 +187,9 @@ cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_o
             const int kchunk = choose_kchunk(P.nz, cols, (long long)device_sms() * std::max(occ, 1));
             dim3 grid((P.nx + 31) / 32, (P.ny + W - 1) / W, (P.nz + kchunk - 1) / kchunk);
             kern<<<grid, dim3(32, W), smem, st>>>(*tmap_adj, lam_next, LX, LY, LZ, LFX, LFY, LFZ, P, kchunk);
+            // one warp per block: the few wall faces spread over every SM
             const long long n0 = (long long)P.ny * P.nz;
-            adj_face_kernel<T, S, 0><<<unsigned((n0 + 127) / 128), 128, 0, st>>>(fb, lam_next, LX, LFX, P, 1);
+            adj_face_kernel<T, S, 0><<<unsigned((n0 + 31) / 32), 32, 0, st>>>(fb, lam_next, LX, LFX, P, 1);
         } else {
             adj_face_kernel<T, S, 0><<<unsigned((nfx + 127) / 128), 128, 0, st>>>(fb, lam_next, LX, LFX, P, 0);
             adj_face_kernel<T, S, 1><<<unsigned((nfc + 127) / 128), 128, 0, st>>>(fb, lam_next, LY, LFY, P, 0);
@@ -199,7 +200,7 @@ cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_o
         T *GH = LFZ + nfc;  // wall-ghost sums, 2 * 19 * ny * nz
         if (!P.periodic_x) {
             const long long ng = 2LL * P.ny * P.nz;
-            adj_ghost_kernel<T, S><<<unsigned((ng + 127) / 128), 128, 0, st>>>(LX, LY, LZ, GH, P);
+            adj_ghost_kernel<T, S><<<unsigned((ng + 31) / 32), 32, 0, st>>>(LX, LY, LZ, GH, P);
         }
         T *MU = GH + 2LL * NPOP * P.ny * P.nz;  // transposed-stencil sums, 19 * nx * ny * nz
         dim3 grid((P.nx + 127) / 128, P.ny, P.nz);
