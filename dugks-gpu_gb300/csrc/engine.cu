@@ -140,6 +140,10 @@ struct dg_ctx {
     CUtensorMap tmap;             // f-bar-plus tensor map of the TMA flux kernel (64-byte aligned type)
     CUtensorMap tmap_adj;         // the same array with the adjoint face kernel's box
     bool have_tmap = false;
+    // CUDA graph of kGraphSteps steps, replayed by dg_run when the step's launch
+    // parameters do not change from step to step (captured on a private stream)
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t step_graph = nullptr;
     long long acc_count = 0;
     bool macro_valid = false;
 
@@ -155,6 +159,13 @@ struct dg_ctx {
         if (dphi) cudaFree(dphi);
         if (acc) cudaFree(acc);
         if (dev_err) cudaFree(dev_err);
+        if (step_graph) cudaGraphExecDestroy(step_graph);
+        if (cap_stream) cudaStreamDestroy(cap_stream);
+    }
+    void drop_graph()
+    {
+        if (step_graph) cudaGraphExecDestroy(step_graph);
+        step_graph = nullptr;
     }
     int fail(int code, const std::string &msg)
     {
@@ -473,8 +484,53 @@ StepParams<T, S> params_for(const dg_ctx *h, int istep)
 // ---------------------------------------------------------------------------
 // per-form dispatch
 // ---------------------------------------------------------------------------
+constexpr int kGraphSteps = 8;
+
+// Steps whose launch parameters are the same every step (no per-step
+// perturbation amplitudes, no per-step rounding seed) can be replayed from a
+// captured graph: kGraphSteps steps cost one graph launch instead of
+// 3 * kGraphSteps kernel launches, which matters for small grids.
+template <class T, class S>
+bool graph_eligible(const dg_ctx *h)
+{
+    if (h->perturb) return false;
+    if (std::is_same<S, __nv_bfloat16>::value && h->stochastic) return false;
+    return true;
+}
+
+template <class T, class S>
+int ensure_step_graph(dg_ctx *h, const StepParams<T, S> &P)
+{
+    using K = Kern<T, S>;
+    if (h->step_graph) return DG_OK;
+    if (!h->cap_stream) CK(cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking), "stream create");
+    S *f = static_cast<S *>(h->f);
+    S *fb = static_cast<S *>(h->fb);
+    CK(cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
+    cudaError_t le = cudaSuccess;
+    for (int s = 0; s < kGraphSteps && le == cudaSuccess; ++s) {
+        le = K::fbar(f, fb, P, h->cap_stream);
+        if (le == cudaSuccess) le = K::flux(fb, f, f, P, h->recon, h->have_tmap ? &h->tmap : nullptr, h->cap_stream);
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(h->cap_stream, &g);
+    if (le != cudaSuccess || ce != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return h->cuda_fail(le != cudaSuccess ? le : ce, "step graph capture");
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&h->step_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+        h->step_graph = nullptr;
+        return h->cuda_fail(ie, "step graph instantiate");
+    }
+    return DG_OK;
+}
+
 // n steps; with `ev` (2n+1 recorded events) the launches are bracketed by
-// CUDA events on the handle's stream for per-kernel timing.
+// CUDA events on the handle's stream for per-kernel timing.  Without events,
+// whole groups of kGraphSteps steps replay the captured step graph where the
+// parameters allow (same kernels, same arguments: identical results).
 template <class T, class S>
 int step_form(dg_ctx *h, int istep0, int n, cudaEvent_t *ev)
 {
@@ -482,8 +538,14 @@ int step_form(dg_ctx *h, int istep0, int n, cudaEvent_t *ev)
     S *f = static_cast<S *>(h->f);
     S *fb = static_cast<S *>(h->fb);
     StepParams<T, S> P = params_for<T, S>(h, istep0);
+    int s = 0;
+    if (!ev && n >= 2 * kGraphSteps && graph_eligible<T, S>(h)) {
+        const int rc = ensure_step_graph<T, S>(h, P);
+        if (rc) return rc;
+        for (; s + kGraphSteps <= n; s += kGraphSteps) CK(cudaGraphLaunch(h->step_graph, h->stream), "graph launch");
+    }
     if (ev) CK(cudaEventRecord(ev[0], h->stream), "event record");
-    for (int s = 0; s < n; ++s) {
+    for (; s < n; ++s) {
         if (h->perturb && s > 0) P = params_for<T, S>(h, istep0 + s);
         set_round_seed<T, S>(h, P.codec, istep0 + s);
         CK(K::fbar(f, fb, P, h->stream), "stage (a) launch");
@@ -1295,6 +1357,7 @@ int dg_adjoint_step(dg_t *h, int istep, const void *f_n, const void *lam_next, v
 int dg_set_force_field(dg_t *h, int axis, const double *phi)
 {
     if (!h) return DG_ERR_ARG;
+    h->drop_graph();  // the captured steps hold the field pointer and axis
     if (!phi) {
         if (h->ffield) CK(cudaFree(h->ffield), "cudaFree (force field)");
         h->ffield = nullptr;

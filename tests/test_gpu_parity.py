@@ -78,6 +78,27 @@ def test_gradient_reconstruction_fp32_matches_oracle(case):
     assert err <= FP32_TOL
 
 
+@pytest.mark.parametrize("shape,periodic_x", [((33, 5, 4), 0), ((65, 3, 2), 0), ((20, 1, 3), 0), ((20, 4, 1), 1),
+                                              ((9, 1, 1), 0)])
+def test_edge_shapes_match_oracle(shape, periodic_x):
+    """Shapes at the edges of the tilings: nx = 1 (mod 32) between walls, a single row
+    or plane (both ghost rows or planes of f-bar-plus are images of it)."""
+    import pydugks
+    import pyoracle
+    from seeded import seeded_state
+    nx, ny, nz = shape
+    cfg = pydugks.make_config(nx=nx, ny=ny, nz=nz, xwidth=nx, ywidth=ny, zwidth=nz, periods_x=periodic_x,
+                              CFL=0.5, visc=0.02, ambient_fx=1e-5 if periodic_x else 0.0, ambient_fz=1e-5)
+    eng = pydugks.Engine(cfg)
+    orc = pyoracle.Oracle.from_engine_info(eng.info)
+    f0 = seeded_state(nx, ny, nz, seed=9)
+    eng.set_state(f0)
+    got, want = run_both(eng, orc, f0, 1, 10)
+    err = rel_err(got, want)
+    print(f"{shape} periodic_x={periodic_x}: rel err {err:.3e}")
+    assert err <= FP64_TOL
+
+
 def test_step_is_deterministic():
     eng, _, f0 = make_pair("walls", "fp64")
     eng.run(1, 5)
@@ -128,3 +149,32 @@ def test_volume_weighted_mass_conserved_stretched():
     eng.run(1, 50)
     m1 = (eng.get_state().sum(axis=-1) * w).sum()
     assert abs(m1 - m0) / m0 < 1e-12
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32", "fp16"])
+def test_graph_replayed_run_equals_single_steps(prec):
+    """dg_run replays captured step graphs (8 steps per launch) when the step's parameters do not
+    change; the result must equal the same steps launched one by one, and a force field set between
+    runs must reach the replayed steps."""
+    import numpy as np
+    from _cases import CASES as C
+    import pydugks
+    from seeded import seeded_state
+    kw = dict(C["walls"])
+    kw["precision"] = prec
+    f0 = seeded_state(kw["nx"], kw["ny"], kw["nz"], seed=14)
+    phi = np.full((kw["nz"], kw["ny"], kw["nx"]), 3e-6)
+    a = pydugks.Engine(pydugks.make_config(**kw))
+    b = pydugks.Engine(pydugks.make_config(**kw))
+    a.set_state(f0)
+    b.set_state(f0)
+    a.run(1, 37)
+    for s in range(1, 38):
+        b.step(s)
+    assert np.array_equal(a.get_state(), b.get_state())
+    a.set_force_field(2, phi)
+    b.set_force_field(2, phi)
+    a.run(38, 21)
+    for s in range(38, 59):
+        b.step(s)
+    assert np.array_equal(a.get_state(), b.get_state())
