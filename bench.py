@@ -385,7 +385,7 @@ def main():
                            "re_tau": 180, "nu": meta["nu"], "alpha": meta["alpha"], "parallelism": f"replicas x{world}",
                            "l2": "inputs larger than L2 (f and f-bar-plus resident, %d MB each)" % (n * 19 * info_bytes // 2**20),
                            "structure": "two-pass (stage a kernel, flux+update kernel)"},
-                "e2e": e2e, "gpu_launches": 3 * K, "roofline": roof, "clocks": clocks}
+                "e2e": e2e, "gpu_launches": (2 if args.precision == "fp32" else 3) * K, "roofline": roof, "clocks": clocks}
         line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:

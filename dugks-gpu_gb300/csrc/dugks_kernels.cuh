@@ -10,7 +10,8 @@
 //                   (src/dugks.cu:348-377, src/parallel.cu:185-234).
 //
 // Kernels:
-//   fbar_kernel      stage (a), src/dugks.cu:1131-1196 (calc_fb1)
+//   fbar_kernel      stage (a), src/dugks.cu:1131-1196 (calc_fb1); in the FP32 form
+//                    also the ghost layer of f-bar-plus
 //   fb_ghost_kernel  x ghost columns of f-bar-plus (periodic images / wall extrapolation)
 //   flux_kernel      stages (c) (d) (e), src/dugks.cu:715-959 (calc_fx_tri) or the
 //                    central-difference variant 421-649 (calc_fx); every face
@@ -199,15 +200,57 @@ __device__ __forceinline__ void cell_force(const StepParams<T, S> &P, int i, int
     }
 }
 
-template <class T, class S>
-__global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *__restrict__ fb, const StepParams<T, S> P)
+// Copies the 19 f-bar-plus values of stored column I, row J, plane K (written
+// by this thread) to their periodic images in y and z when ny or nz is 1, so
+// that both ghost rows (planes) are images of the one interior row (plane).
+template <class S>
+__device__ __forceinline__ void copy_images(S *fb, long long ps_b, int I, int J, int K, int ny, int nz, int pitch_b)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int js[3], ks[3], nj = 0, nk = 0;
+    js[nj++] = J;
+    if (J == 1) js[nj++] = ny + 1;
+    if (J == ny) js[nj++] = 0;
+    ks[nk++] = K;
+    if (K == 1) ks[nk++] = nz + 1;
+    if (K == nz) ks[nk++] = 0;
+    const long long src = ((long long)K * (ny + 2) + J) * pitch_b + I;
+    for (int p = 0; p < NPOP; ++p) {
+        const S v = fb[p * ps_b + src];
+        for (int a = 0; a < nk; ++a)
+            for (int b = 0; b < nj; ++b)
+                if (a || b) fb[p * ps_b + ((long long)ks[a] * (ny + 2) + js[b]) * pitch_b + I] = v;
+    }
+}
+
+// Stage (a) for one cell.  GHOST = false: the interior of f-bar-plus only
+// (fb_ghost_kernel fills the ghost layer).  GHOST = true: the ghost layer is
+// written by the threads that hold its sources, in the same launch -- a cell
+// of the first/last row or plane also writes its periodic images in y and z
+// (src/dugks.cu:1256-1273, src/parallel.cu:192-199), the first/last cell of a
+// row writes the periodic x copy (src/dugks.cu:1212-1229), and between walls
+// each warp next to a wall forms the extrapolation g0 = q0 fb(1) + (1-q0) fb(2),
+// g_{nx+1} = q1 fb(nx) + (1-q1) fb(nx-1) of the stored values (src/dugks.cu:1234-1251;
+// stretched mesh src/fortran/channel/src/dugks.cuf:365-374), one population per
+// lane.  Warps away from walls, x ends and boundary rows/planes take the
+// plain path.  xoff shifts the cells by one thread when nx = 1 (mod 32) so
+// that cells nx-1 and nx share a warp.  The result equals the reference's
+// x -> y -> z fill order.
+template <class T, class S, bool GHOST>
+__global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *__restrict__ fb, const StepParams<T, S> P,
+                                                   int xoff)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x - xoff;
     const int j = blockIdx.y;
     const int k = blockIdx.z;
-    if (i >= P.nx) return;
-    const long long c = ((long long)k * P.ny + j) * P.pitch + i;
-    const long long cb = ((long long)(k + 1) * (P.ny + 2) + (j + 1)) * P.pitch_b + i + 1;
+    const int nx = P.nx, ny = P.ny, nz = P.nz;
+    const bool in = i >= 0 && i < nx;
+    const int wbase = blockIdx.x * blockDim.x + (threadIdx.x & ~31) - xoff;  // cell of lane 0
+    const bool wall_warp =
+        GHOST && !P.periodic_x && ((wbase <= 1 && wbase + 31 >= 0) || (wbase <= nx - 1 && wbase + 31 >= nx - 2));
+    if (!in && !wall_warp) return;
+    const int ic = in ? i : (i < 0 ? 0 : nx - 1);  // lanes past the row read a valid cell and store nothing
+    const long long c = ((long long)k * ny + j) * P.pitch + ic;
+    const long long cb = ((long long)(k + 1) * (ny + 2) + (j + 1)) * P.pitch_b + ic + 1;
 
     T v[NPOP];
 #pragma unroll
@@ -219,7 +262,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     T u = jx * inv, vv = jy * inv, w = jz * inv;
 
     T Fx, Fy, Fz;
-    cell_force(P, i, j, k, Fx, Fy, Fz);
+    cell_force(P, ic, j, k, Fx, Fy, Fz);
     const bool forced = P.force_on || P.perturb || P.ffield;
     if (forced) {
         u = fma(P.hdt, Fx, u);
@@ -233,9 +276,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     T fe[NPOP];
     feq_all(r, u, vv, w, fe);
     const unsigned hc = P.codec.cell_hash(cb);
-
-#pragma unroll
-    for (int p = 0; p < NPOP; ++p) {
+    auto fbar_p = [&](int p) -> T {
         T K = P.Kb[p];
         if (P.perturb || P.ffield) {
             T cf = T(0);
@@ -244,8 +285,70 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
             if (cz(p)) cf += cz(p) > 0 ? Fz : -Fz;
             K = P.bw0x3 * cf;
         }
-        const T out = fma(B + K, fe[p], P.bw1 * v[p]);
-        P.codec.store_h(fb, p * P.ps_b + cb, p, out, hc);
+        return fma(B + K, fe[p], P.bw1 * v[p]);
+    };
+
+    // periodic images of this row and plane (uniform over the warp): J = 1 -> ny+1,
+    // J = ny -> 0, likewise K, and the corner image
+    const long long rstep = P.pitch_b, pstep = (long long)(ny + 2) * P.pitch_b;
+    const long long dj = j == 0 ? ny * rstep : (j == ny - 1 ? -(long long)ny * rstep : 0);
+    const long long dk = k == 0 ? nz * pstep : (k == nz - 1 ? -(long long)nz * pstep : 0);
+    const bool small = ny == 1 || nz == 1;  // two images along one axis: copied at the end
+    const bool img = !small && (dj != 0 || dk != 0);
+    const bool xend = wbase <= 0 || wbase + 31 >= nx - 1;
+    if (!GHOST || (!wall_warp && !img && !small && !(P.periodic_x && xend))) {
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) fb[p * P.ps_b + cb] = P.codec.encode_h(p, fbar_p(p), hc);
+        return;
+    }
+    __shared__ T wv[4][4][NPOP];  // per warp: values of cells 1, 2, nx, nx-1 (blocks of at most 128 threads)
+    auto put = [&](S *q, S val) {  // a value and its images
+        q[0] = val;
+        if (img) {
+            if (dj) q[dj] = val;
+            if (dk) q[dk] = val;
+            if (dj && dk) q[dj + dk] = val;
+        }
+    };
+    const long long rowb = cb - (ic + 1);  // stored column 0 of this row and plane
+    const int wl = threadIdx.x >> 5;
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) {
+        const T out = fbar_p(p);
+        S *pl = fb + p * P.ps_b + rowb;
+        const S e = P.codec.encode_h(p, out, hc);
+        if (in) {
+            put(pl + ic + 1, e);
+            if (P.periodic_x) {
+                if (ic == 0) put(pl + nx + 1, e);
+                if (ic == nx - 1) put(pl, e);
+            }
+        }
+        if (wall_warp) {
+            // the stored values of the two cells next to each wall
+            const T mine = Codec<T, S>::deviation ? P.codec.dec(p, T(e)) : out;
+            if (in && ic == 0) wv[wl][0][p] = mine;
+            if (in && ic == 1) wv[wl][1][p] = mine;
+            if (in && ic == nx - 1) wv[wl][2][p] = mine;
+            if (in && ic == nx - 2) wv[wl][3][p] = mine;
+        }
+    }
+    if (wall_warp) {
+        __syncwarp();
+        const int lane = threadIdx.x & 31;
+        if (lane < NPOP) {
+            const int p = lane;
+            S *pl = fb + p * P.ps_b + rowb;
+            if (wbase <= 0) put(pl, P.codec.encode_h(p, P.q0 * wv[wl][0][p] + (T(1) - P.q0) * wv[wl][1][p], hc));
+            if (wbase + 31 >= nx - 1)
+                put(pl + nx + 1, P.codec.encode_h(p, P.q1 * wv[wl][2][p] + (T(1) - P.q1) * wv[wl][3][p], hc));
+        }
+        __syncwarp();
+    }
+    if (small && in) {
+        copy_images(fb, P.ps_b, ic + 1, j + 1, k + 1, ny, nz, P.pitch_b);
+        if (ic == 0) copy_images(fb, P.ps_b, P.periodic_x ? nx + 1 : 0, j + 1, k + 1, ny, nz, P.pitch_b);
+        if (ic == nx - 1) copy_images(fb, P.ps_b, P.periodic_x ? 0 : nx + 1, j + 1, k + 1, ny, nz, P.pitch_b);
     }
 }
 

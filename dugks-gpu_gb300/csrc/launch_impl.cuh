@@ -10,11 +10,22 @@ namespace dg {
 template <class T, class S>
 cudaError_t Kern<T, S>::fbar(const S *f, S *fb, const StepParams<T, S> &P, cudaStream_t st)
 {
-    const int bx = P.nx >= 128 ? 128 : ((P.nx + 31) / 32) * 32;
-    dim3 grid((P.nx + bx - 1) / bx, P.ny, P.nz);
-    fbar_kernel<T, S><<<grid, bx, 0, st>>>(f, fb, P);
-    const long long ghosts = 2LL * (P.ny + 2) * (P.nz + 2) + 2LL * P.nx * (P.nz + 2) + 2LL * P.nx * P.ny;
-    fb_ghost_kernel<T, S><<<unsigned((ghosts + 255) / 256), 256, 0, st>>>(fb, P);
+    if constexpr (std::is_same<S, float>::value) {
+        // FP32: stage (a) writes the ghost layer itself (one launch); cells nx-1 and nx
+        // must share a warp for the wall extrapolation: shift by one when nx = 1 (mod 32)
+        const int xoff = (!P.periodic_x && P.nx % 32 == 1) ? 1 : 0;
+        const int bx = P.nx + xoff >= 128 ? 128 : ((P.nx + xoff + 31) / 32) * 32;
+        dim3 grid((P.nx + xoff + bx - 1) / bx, P.ny, P.nz);
+        fbar_kernel<T, S, true><<<grid, bx, 0, st>>>(f, fb, P, xoff);
+    } else {
+        // FP64 and 16-bit storage: the fused ghost writes cost more issue in stage (a)
+        // (FP64 pipe, 16-bit encode) than the separate pass saves
+        const int bx = P.nx >= 128 ? 128 : ((P.nx + 31) / 32) * 32;
+        dim3 grid((P.nx + bx - 1) / bx, P.ny, P.nz);
+        fbar_kernel<T, S, false><<<grid, bx, 0, st>>>(f, fb, P, 0);
+        const long long ghosts = 2LL * (P.ny + 2) * (P.nz + 2) + 2LL * P.nx * (P.nz + 2) + 2LL * P.nx * P.ny;
+        fb_ghost_kernel<T, S><<<unsigned((ghosts + 255) / 256), 256, 0, st>>>(fb, P);
+    }
     return cudaGetLastError();
 }
 

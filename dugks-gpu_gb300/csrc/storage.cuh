@@ -27,6 +27,7 @@ struct Codec {
     __device__ __forceinline__ T load_s(const S *a, int idx, int) const { return T(a[idx]); }
     __device__ __forceinline__ void store(S *a, long long idx, int, T v) const { a[idx] = S(v); }
     __device__ __forceinline__ unsigned cell_hash(long long) const { return 0u; }
+    __device__ __forceinline__ S encode_h(int, T v, unsigned) const { return S(v); }
     __device__ __forceinline__ void store_h(S *a, long long idx, int p, T v, unsigned) const { store(a, idx, p, v); }
     // undecoded reads and the decode of a value affine in them (identity here)
     __device__ __forceinline__ T raw_nc(const S *a, long long idx) const { return T(__ldg(a + idx)); }
@@ -74,6 +75,10 @@ struct Codec<float, __half> : DevCodec<__half> {
         a[idx] = __float2half_rn((v - w[p]) * is[p]);
     }
     __device__ __forceinline__ unsigned cell_hash(long long) const { return 0u; }
+    __device__ __forceinline__ __half encode_h(int p, float v, unsigned) const
+    {
+        return __float2half_rn((v - w[p]) * is[p]);
+    }
     __device__ __forceinline__ void store_h(__half *a, long long idx, int p, float v, unsigned) const
     {
         store(a, idx, p, v);
@@ -113,15 +118,16 @@ struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
     {
         return sr_seed ? (mix32(unsigned(cell) ^ sr_seed) | 1u) : 0u;
     }
-    __device__ __forceinline__ void store_h(__nv_bfloat16 *a, long long idx, int p, float v, unsigned h) const
+    __device__ __forceinline__ __nv_bfloat16 encode_h(int p, float v, unsigned h) const
     {
         const float d = (v - w[p]) * is[p];
-        if (h == 0u) {
-            a[idx] = __float2bfloat16_rn(d);
-            return;
-        }
+        if (h == 0u) return __float2bfloat16_rn(d);
         const unsigned r = (h * (0x9e3779b1u + 0x6a09e66eu * unsigned(p))) >> 16;  // odd multiplier per p
-        a[idx] = __ushort_as_bfloat16((unsigned short)((__float_as_uint(d) + r) >> 16));
+        return __ushort_as_bfloat16((unsigned short)((__float_as_uint(d) + r) >> 16));
+    }
+    __device__ __forceinline__ void store_h(__nv_bfloat16 *a, long long idx, int p, float v, unsigned h) const
+    {
+        a[idx] = encode_h(p, v, h);
     }
     __device__ __forceinline__ float raw_nc(const __nv_bfloat16 *a, long long idx) const
     {
