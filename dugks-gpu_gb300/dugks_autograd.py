@@ -48,6 +48,22 @@ def to_dump_order(eng, t):
     return soa_view(eng, t).permute(1, 2, 3, 0)
 
 
+class _DeviceBuffer:
+    """A CUDA array interface over a raw device pointer (no ownership, no copy)."""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (int(ptr), False),
+                                         "strides": None, "version": 3}
+
+
+def engine_state(eng):
+    """Tensor view of the engine's own state buffer (DG_BUF_F, SoA layout): it
+    follows the state as steps run on the engine's stream; no copy."""
+    dt = state_dtype(eng)
+    buf = _DeviceBuffer(eng.device_ptr(pydugks.DG_BUF_F), eng.soa_len, "<f8" if dt == torch.float64 else "<f4")
+    return torch.as_tensor(buf, device="cuda")
+
+
 def _sync_stream(eng):
     eng.set_stream(torch.cuda.current_stream().cuda_stream)
 
@@ -119,16 +135,17 @@ class DugksObjectiveRun(torch.autograd.Function):
         end, last = revolve.spine(acts)
         stored = {0: f0.detach().clone()}
         eng.set_state_device(f0.data_ptr())
-        cur = empty_state(eng, f0.device)
         J = torch.zeros((), dtype=torch.float64, device=f0.device)
         phi_d = phi.detach()
+        state = engine_state(eng)
+        # objectives with `prepare(phi)` give a per-state evaluator for the fixed control
+        value = objective.prepare(phi_d) if hasattr(objective, "prepare") else (lambda s: objective(s, phi_d))
 
         def advance(a, b):
             for k in range(a, b):
                 eng.step(istep0 + k)
-                eng.get_state_device(cur.data_ptr())
                 with torch.no_grad():
-                    J.add_(objective(cur, phi_d).double())
+                    J.add_(value(state).double())
 
         k = 0
         for a in acts[:end]:
@@ -162,7 +179,7 @@ class DugksObjectiveRun(torch.autograd.Function):
         else:
             lam = lam_out.detach().contiguous().clone()
         dphi_direct = torch.zeros(phi.shape, dtype=torch.float64, device=phi.device)
-        cur = empty_state(eng, lam.device)
+        cur = engine_state(eng)  # the engine's current state (read by the adjoint and the sources)
 
         def source(state):
             nonlocal dphi_direct
@@ -171,7 +188,7 @@ class DugksObjectiveRun(torch.autograd.Function):
                 dphi_direct += acc(lam, state, phi.detach(), w).double()
                 return
             with torch.enable_grad():
-                s = state.detach().requires_grad_(True)
+                s = state.detach().clone().requires_grad_(True)
                 p = phi.detach().requires_grad_(True)
                 g = objective(s, p).double() * w
                 gs, gp = torch.autograd.grad(g, [s, p], allow_unused=True)
@@ -183,7 +200,6 @@ class DugksObjectiveRun(torch.autograd.Function):
         # source at the final state f_n
         eng.set_state_device(stored[ctx.last].data_ptr())
         eng.run(istep0 + ctx.last, n - ctx.last) if n > ctx.last else None
-        eng.get_state_device(cur.data_ptr())
         source(cur)
         # resume the schedule from the last state of the forward sweep
         eng.set_state_device(stored[ctx.last].data_ptr())
@@ -199,9 +215,8 @@ class DugksObjectiveRun(torch.autograd.Function):
                 eng.set_state_device(stored[a[1]].data_ptr())
             elif kind == "release":
                 stored.pop(a[1], None)
-            else:  # adjoint of step k at the current state k
+            else:  # adjoint of step k at the current state k (the engine's own buffer)
                 k = a[1]
-                eng.get_state_device(cur.data_ptr())
                 eng.adjoint_step(istep0 + k, cur.data_ptr(), lam.data_ptr(), lam.data_ptr())
                 if k >= 1:
                     source(cur)
@@ -243,6 +258,24 @@ class WallShear:
     def _planes(self, t):
         v = soa_view(self.eng, t)
         return v[..., 0], v[..., self.eng.nx - 1]   # (19, nz, ny) each
+
+    def prepare(self, phi):
+        """Evaluator of the objective for a fixed field phi: the objective is a
+        weighted sum over the two wall planes, weights (nu/d)(c_s + hdt F_s)/area
+        formed once; each evaluation is one gather and one FP64 reduction."""
+        nx = self.eng.nx
+        dev = phi.device
+        cs = self.cs.to(torch.float64).to(dev).view(19, 1, 1, 1)
+        ph = phi[:, :, [0, nx - 1]].double()                                  # (nz, ny, 2)
+        wd = torch.tensor([self.nu / self.d0, self.nu / self.d1], dtype=torch.float64, device=dev)
+        W = (cs + self.hdt * (self.F + ph).unsqueeze(0)) * wd / self.area      # (19, nz, ny, 2)
+        idx = torch.tensor([0, nx - 1], device=dev)
+
+        def value(state):
+            planes = soa_view(self.eng, state).index_select(3, idx)          # (19, nz, ny, 2)
+            return (planes.double() * W).sum()
+
+        return value
 
     def __call__(self, state, phi):
         lo, hi = self._planes(state)
