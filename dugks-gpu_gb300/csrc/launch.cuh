@@ -26,8 +26,8 @@ struct TileCfg<float, float> {
 };
 template <>
 struct TileCfg<double, double> {
-    static constexpr int W = 8;       // 7 rows; the FP64 kernel takes 255 registers at 256 threads
-    static constexpr int MINB = 1;
+    static constexpr int W = 8;       // 7 rows, two CTAs per SM: 128 registers with spills, but 16
+    static constexpr int MINB = 2;    // warps per SM keep the FP64 pipe busier (+5 % over one CTA at 255)
     static constexpr bool TMA = false;
 };
 
