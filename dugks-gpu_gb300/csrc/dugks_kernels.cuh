@@ -34,6 +34,26 @@ namespace dg {
 // Parameters (host-filled, passed by value; T-typed so that no conversion from
 // double runs in an FP32 kernel)
 // ---------------------------------------------------------------------------
+// Rows of the corner-weight table (products of the face_tri lerp weights that
+// involve an x weight; column = face index I for the x-face rows, cell column
+// for the y- and z-face rows).  class = xrep(p).
+constexpr int CW_XY = 0;     // + 4 (class-1) + q   x face, c_y != 0 = c_z
+constexpr int CW_XZ = 12;    // + 4 (class-1) + q   x face, c_z != 0 = c_y
+constexpr int CW_XYZ = 24;   // + q (q < 8)         x face, c_y, c_z != 0 (c_x = 0)
+constexpr int CW_Y4 = 32;    // + 4 slot4y(p) + q   y face, c_x != 0 = c_z (p = 1, 2, 7..10)
+constexpr int CW_Y8 = 56;    // + 8 (class-1) + q   y face, c_x, c_z != 0 (c_y = 0)
+constexpr int CW_Z4 = 72;    // + 4 slot4z(p) + q   z face, c_x != 0 = c_y (p = 1, 2, 11..14)
+constexpr int CW_Z8 = 96;    // + 8 (class-1) + q   z face, c_x, c_y != 0 (c_z = 0)
+constexpr int CW_ROWS = 112;
+__host__ __device__ constexpr int slot4y(int p) { return p == 1 ? 0 : (p == 2 ? 1 : p - 5); }
+__host__ __device__ constexpr int slot4z(int p) { return p == 1 ? 0 : (p == 2 ? 1 : p - 9); }
+
+// The corner-weight faces are used where the FP64 pipe bounds the step.
+template <class T>
+struct CornerWeights { static constexpr bool value = false; };
+template <>
+struct CornerWeights<double> { static constexpr bool value = true; };
+
 template <class T, class S>
 struct StepParams {
     int nx, ny, nz, pitch;
@@ -52,6 +72,7 @@ struct StepParams {
     T hF[3];                     // (0.5*hdt)*F, the face velocity shift (src/dugks.cu:698-700)
     T Kf[NPOP];                  // 3*fw0*(c_p . F)
     T fw2s, fw0x3s, Kfs[NPOP];   // fw2, 3*fw0, Kf divided by fw1 (fluxes are kept divided by fw1)
+    T bwF;                       // bw2*hdt + bw0: momentum of f-bar-plus = j + rho F bwF (exact arithmetic)
     T cyuf, czuf;                // fw1*dt/dy, fw1*dt/dz
     // interpolation weights, (1-m, m) pairs in the reference's lerp form
     T ty_om, ty_m;               // transverse y, |hdt/dy|
@@ -62,6 +83,9 @@ struct StepParams {
     T q0, q1;                    // wall ghost extrapolation weights (2 on a uniform mesh)
     T g_idx, g_idy, g_idz;       // gradient reconstruction: 1/dx, 1/dy, 1/dz
     T g_i2dx, g_i2dy, g_i2dz;    // 1/(2dx), 1/(2dy), 1/(2dz)
+    T ycw[NPOP][4];              // y face, c_x = 0, c_z != 0: z-lerp x y-lerp weight products
+    T zcw[NPOP][4];              // z face, c_x = 0, c_y != 0: z-lerp x y-lerp weight products
+    const T *cw;                 // [CW_ROWS][xws] corner weights of the FP64 faces (face_tri_cw)
     const T *xw;                 // [19*2][xws] x-face normal (1-m, m) of face I (between cells I, I+1, 1-based)
     const T *txw;                // [19*2][xws] transverse x (1-t, t) per column 0..nx+1
     int xws;                     // row stride of xw / txw (nx+2)
@@ -91,13 +115,14 @@ __device__ __forceinline__ T lerp2(T om, T m, T a, T b)
 
 // Equilibrium of the pair (p, opp(p)) from eu = 3 c_p.u, base = 1 - 1.5|u|^2
 // and wr = w_p*rho:  feq = wr*(1 + eu + eu^2/2 - 1.5|u|^2)
-// (src/dugks.cu:1201-1207 with 1/RT = 3).
+// (src/dugks.cu:1201-1207 with 1/RT = 3), as wr*t +- wr*eu: five operations
+// for the pair.
 template <class T>
 __device__ __forceinline__ void feq_pair(T eu, T base, T wr, T &fp, T &fm)
 {
-    const T t = fma(T(0.5) * eu, eu, base);
-    fp = wr * (t + eu);
-    fm = wr * (t - eu);
+    const T wt = wr * fma(T(0.5) * eu, eu, base);
+    fp = fma(wr, eu, wt);
+    fm = fma(-wr, eu, wt);
 }
 
 // Zeroth and first moments of 19 values.  Summed as balanced trees (the
@@ -131,6 +156,16 @@ __device__ __forceinline__ double recip(double r)
     return fma(x, e, x);
 }
 __device__ __forceinline__ float recip(float r) { return __frcp_rn(r); }
+
+// First term of the update, 4/3 f-bar-plus - 1/3 f (src/dugks.cu:954).  FP64:
+// as written.  FP32 arithmetic: fb + (fb - f)/3, whose coefficients sum to one
+// exactly; float(4/3) - float(1/3) = 1 + 3e-8 would make the mass and momentum
+// grow by that factor every step (the reference evaluates this line in double).
+template <class T>
+__device__ __forceinline__ T upd_base(T fb, T fo, T c43, T c13)
+{
+    return sizeof(T) == 8 ? fma(fb, c43, -(fo * c13)) : fma(fb - fo, c13, fb);
+}
 
 // All 19 equilibria for density r and velocity (u, v, w).
 template <class T>
@@ -287,6 +322,33 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
         }
         return fma(B + K, fe[p], P.bw1 * v[p]);
     };
+    T ob[NPOP];
+#pragma unroll
+    for (int p = 0; p < NPOP; ++p) ob[p] = fbar_p(p);
+    if (sizeof(T) == 4) {
+        // FP32 arithmetic: the moments of f-bar-plus are set to their exact values
+        // (exact arithmetic: sum f-bar-plus = rho, sum c f-bar-plus = j + rho F
+        // (bw2 hdt + bw0)).  The float weights and bw1, bw2 carry rounding biases
+        // of ~1e-8 that would otherwise add up, step after step, into a drift of
+        // the total mass and momentum.  The momentum defect goes to the +- pair of
+        // each axis (mass unchanged), the mass defect to the rest population.
+        T r2, mx, my, mz;
+        moments(ob, r2, mx, my, mz);
+        T tx = jx, ty = jy, tz = jz;
+        if (forced) {
+            const T g = r * P.bwF;
+            tx = fma(g, Fx, jx);
+            ty = fma(g, Fy, jy);
+            tz = fma(g, Fz, jz);
+        }
+        const T dx = T(0.5) * (tx - mx), dy = T(0.5) * (ty - my), dz = T(0.5) * (tz - mz);
+        ob[1] += dx; ob[2] -= dx;
+        ob[3] += dy; ob[4] -= dy;
+        ob[5] += dz; ob[6] -= dz;
+        const T a = (ob[1] + ob[2]) + (ob[3] + ob[4]), b = (ob[5] + ob[6]) + (ob[7] + ob[8]);
+        const T c2 = (ob[9] + ob[10]) + (ob[11] + ob[12]), d = (ob[13] + ob[14]) + (ob[15] + ob[16]);
+        ob[0] = r - ((((a + b) + (c2 + d)) + ob[17]) + ob[18]);
+    }
 
     // periodic images of this row and plane (uniform over the warp): J = 1 -> ny+1,
     // J = ny -> 0, likewise K, and the corner image
@@ -298,7 +360,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     const bool xend = wbase <= 0 || wbase + 31 >= nx - 1;
     if (!GHOST || (!wall_warp && !img && !small && !(P.periodic_x && xend))) {
 #pragma unroll
-        for (int p = 0; p < NPOP; ++p) fb[p * P.ps_b + cb] = P.codec.encode_h(p, fbar_p(p), hc);
+        for (int p = 0; p < NPOP; ++p) fb[p * P.ps_b + cb] = P.codec.encode_h(p, ob[p], hc);
         return;
     }
     __shared__ T wv[4][4][NPOP];  // per warp: values of cells 1, 2, nx, nx-1 (blocks of at most 128 threads)
@@ -314,7 +376,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     const int wl = threadIdx.x >> 5;
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
-        const T out = fbar_p(p);
+        const T out = ob[p];
         S *pl = fb + p * P.ps_b + rowb;
         const S e = P.codec.encode_h(p, out, hc);
         if (in) {
@@ -559,6 +621,142 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
     }
 }
 
+// Corner-weight form of face_tri for the FP64 step, whose throughput is set by
+// the FP64 instruction count: each face value is sum_q w_q f_q over its 2, 4
+// or 8 stencil points (one multiply and FMAs) instead of the nested lerps
+// (two operations per lerp: 6 for a bilinear, 14 for a trilinear value).  The
+// weights are the products of the lerp weights, from the corner-weight table
+// P.cw (rows of the CW_* layout, column-dependent through the x weights) and,
+// where no x weight enters, from the uniform products in P.ycw / P.zcw.  Same
+// stencil points and weights as face_tri; the sums differ only by rounding.
+template <class T, class S, int AX, class RD>
+__device__ __forceinline__ void face_tri_cw(const StepParams<T, S> &P, const RD &R, int i, int j, int k, T v[NPOP])
+{
+    using RI = decltype(R.rb(0, 0));
+    const int jm = j - 1, jp = j + 1, jc = j;
+    const int km = k - 1, kp = k + 1, kc = k;
+    const int xs = P.xws;
+    const T *cw = P.cw + i;
+    if (AX == 0) {
+        const int A = i == 0 ? 1 : i, B = i == 0 ? 0 : i + 1;
+        const T *xw = P.xw + i;
+        const RI r00 = R.rb(jc, kc);
+        v[0] = R.dec(0, T(0.5) * (R.raw(0, r00, A) + R.raw(0, r00, B)));
+#pragma unroll
+        for (int p = 1; p < NPOP; ++p) {
+            const int ay = cy(p), az = cz(p), c = xrep(p);
+            const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
+            const int kt = az > 0 ? km : (az < 0 ? kp : kc);
+            T t;
+            if (!ay && !az) {
+                t = lerp2(__ldg(xw + (2 * c) * xs), __ldg(xw + (2 * c + 1) * xs), R.raw(p, r00, A), R.raw(p, r00, B));
+            } else if (!az) {
+                const RI r10 = R.rb(jt, kc);
+                const T *w = cw + (CW_XY + 4 * (c - 1)) * xs;
+                t = __ldg(w) * R.raw(p, r00, A);
+                t = fma(__ldg(w + xs), R.raw(p, r00, B), t);
+                t = fma(__ldg(w + 2 * xs), R.raw(p, r10, A), t);
+                t = fma(__ldg(w + 3 * xs), R.raw(p, r10, B), t);
+            } else if (!ay) {
+                const RI r01 = R.rb(jc, kt);
+                const T *w = cw + (CW_XZ + 4 * (c - 1)) * xs;
+                t = __ldg(w) * R.raw(p, r00, A);
+                t = fma(__ldg(w + xs), R.raw(p, r00, B), t);
+                t = fma(__ldg(w + 2 * xs), R.raw(p, r01, A), t);
+                t = fma(__ldg(w + 3 * xs), R.raw(p, r01, B), t);
+            } else {
+                const RI r10 = R.rb(jt, kc), r01 = R.rb(jc, kt), r11 = R.rb(jt, kt);
+                const T *w = cw + CW_XYZ * xs;
+                t = __ldg(w) * R.raw(p, r00, A);
+                t = fma(__ldg(w + xs), R.raw(p, r00, B), t);
+                t = fma(__ldg(w + 2 * xs), R.raw(p, r10, A), t);
+                t = fma(__ldg(w + 3 * xs), R.raw(p, r10, B), t);
+                t = fma(__ldg(w + 4 * xs), R.raw(p, r01, A), t);
+                t = fma(__ldg(w + 5 * xs), R.raw(p, r01, B), t);
+                t = fma(__ldg(w + 6 * xs), R.raw(p, r11, A), t);
+                t = fma(__ldg(w + 7 * xs), R.raw(p, r11, B), t);
+            }
+            v[p] = R.dec(p, t);
+        }
+    } else if (AX == 1) {
+        // rows j (A) and j+1 (B); transverse x to column i - cx, z to plane k - cz
+        const RI rA = R.rb(jc, kc), rB = R.rb(jp, kc);
+        v[0] = R.dec(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+#pragma unroll
+        for (int p = 1; p < NPOP; ++p) {
+            const int ax = cx(p), az = cz(p), c = xrep(p);
+            const int io = i - ax;
+            const int kt = az > 0 ? km : (az < 0 ? kp : kc);
+            T t;
+            if (!ax && !az) {
+                t = lerp2(P.yn_om[p], P.yn_m[p], R.raw(p, rA, i), R.raw(p, rB, i));
+            } else if (!az) {
+                const T *w = cw + (CW_Y4 + 4 * slot4y(p)) * xs;
+                t = __ldg(w) * R.raw(p, rA, i);
+                t = fma(__ldg(w + xs), R.raw(p, rA, io), t);
+                t = fma(__ldg(w + 2 * xs), R.raw(p, rB, i), t);
+                t = fma(__ldg(w + 3 * xs), R.raw(p, rB, io), t);
+            } else if (!ax) {
+                const RI sA = R.rb(jc, kt), sB = R.rb(jp, kt);
+                t = P.ycw[p][0] * R.raw(p, rA, i);
+                t = fma(P.ycw[p][1], R.raw(p, rB, i), t);
+                t = fma(P.ycw[p][2], R.raw(p, sA, i), t);
+                t = fma(P.ycw[p][3], R.raw(p, sB, i), t);
+            } else {
+                const RI sA = R.rb(jc, kt), sB = R.rb(jp, kt);
+                const T *w = cw + (CW_Y8 + 8 * (c - 1)) * xs;
+                t = __ldg(w) * R.raw(p, rA, i);
+                t = fma(__ldg(w + xs), R.raw(p, rA, io), t);
+                t = fma(__ldg(w + 2 * xs), R.raw(p, rB, i), t);
+                t = fma(__ldg(w + 3 * xs), R.raw(p, rB, io), t);
+                t = fma(__ldg(w + 4 * xs), R.raw(p, sA, i), t);
+                t = fma(__ldg(w + 5 * xs), R.raw(p, sA, io), t);
+                t = fma(__ldg(w + 6 * xs), R.raw(p, sB, i), t);
+                t = fma(__ldg(w + 7 * xs), R.raw(p, sB, io), t);
+            }
+            v[p] = R.dec(p, t);
+        }
+    } else {
+        // planes k (A) and k+1 (B); transverse x to column i - cx, y to row j - cy
+        const RI rA = R.rb(jc, kc), rB = R.rb(jc, kp);
+        v[0] = R.dec(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+#pragma unroll
+        for (int p = 1; p < NPOP; ++p) {
+            const int ax = cx(p), ay = cy(p), c = xrep(p);
+            const int io = i - ax;
+            const int jt = ay > 0 ? jm : (ay < 0 ? jp : jc);
+            T t;
+            if (!ax && !ay) {
+                t = lerp2(P.zn_om[p], P.zn_m[p], R.raw(p, rA, i), R.raw(p, rB, i));
+            } else if (!ay) {
+                const T *w = cw + (CW_Z4 + 4 * slot4z(p)) * xs;
+                t = __ldg(w) * R.raw(p, rA, i);
+                t = fma(__ldg(w + xs), R.raw(p, rA, io), t);
+                t = fma(__ldg(w + 2 * xs), R.raw(p, rB, i), t);
+                t = fma(__ldg(w + 3 * xs), R.raw(p, rB, io), t);
+            } else if (!ax) {
+                const RI sA = R.rb(jt, kc), sB = R.rb(jt, kp);
+                t = P.zcw[p][0] * R.raw(p, rA, i);
+                t = fma(P.zcw[p][1], R.raw(p, sA, i), t);
+                t = fma(P.zcw[p][2], R.raw(p, rB, i), t);
+                t = fma(P.zcw[p][3], R.raw(p, sB, i), t);
+            } else {
+                const RI sA = R.rb(jt, kc), sB = R.rb(jt, kp);
+                const T *w = cw + (CW_Z8 + 8 * (c - 1)) * xs;
+                t = __ldg(w) * R.raw(p, rA, i);
+                t = fma(__ldg(w + xs), R.raw(p, rA, io), t);
+                t = fma(__ldg(w + 2 * xs), R.raw(p, sA, i), t);
+                t = fma(__ldg(w + 3 * xs), R.raw(p, sA, io), t);
+                t = fma(__ldg(w + 4 * xs), R.raw(p, rB, i), t);
+                t = fma(__ldg(w + 5 * xs), R.raw(p, rB, io), t);
+                t = fma(__ldg(w + 6 * xs), R.raw(p, sB, i), t);
+                t = fma(__ldg(w + 7 * xs), R.raw(p, sB, io), t);
+            }
+            v[p] = R.dec(p, t);
+        }
+    }
+}
+
 // 19 face values of the central-difference ("gradient") reconstruction,
 // f_face = mean - hdt (c . grad), src/dugks.cu:459-583 (calc_fx): normal
 // gradient across the face, transverse gradients of face-averaged neighbours
@@ -714,7 +912,9 @@ template <class T, class S, int AX, int RECON, bool FF, class RD>
 __device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const RD &R, int i, int j, int k, T out[10])
 {
     T v[NPOP];
-    if (RECON == 0)
+    if (RECON == 0 && CornerWeights<T>::value)
+        face_tri_cw<T, S, AX>(P, R, i, j, k, v);
+    else if (RECON == 0)
         face_tri<T, S, AX>(P, R, i, j, k, v);
     else
         face_grad<T, S, AX>(P, R, i, j, k, v);
@@ -785,7 +985,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict_
 #pragma unroll
                 for (int p = 0; p < NPOP; ++p) {
                     const T fo = P.codec.load(f_in, p * P.ps + c, p);
-                    T r = fma(R(p, cb, 0), c43, -(fo * c13));
+                    T r = upd_base(R(p, cb, 0), fo, c43, c13);
                     if (cx(p)) {
                         const int s = flux_slot(0, p);
                         r = fma(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s], r);
@@ -965,7 +1165,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
                 const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
 #pragma unroll
                 for (int p = 0; p < NPOP; ++p) {
-                    T r = fma(R(p, cb, 0), c43, -(fo[p] * c13));
+                    T r = upd_base(R(p, cb, 0), fo[p], c43, c13);
                     if (cx(p)) {
                         const int s = flux_slot(0, p);
                         r = fma(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s], r);

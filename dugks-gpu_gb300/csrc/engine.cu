@@ -126,8 +126,8 @@ struct dg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     void *f = nullptr, *fb = nullptr;
-    void *tab = nullptr;          // xw | txw | cxu | pert_x | pert_y | pert_z | cxuf (T-typed)
-    size_t tab_off[7] = {};
+    void *tab = nullptr;          // xw | txw | cxu | pert_x | pert_y | pert_z | cxuf | cw (T-typed)
+    size_t tab_off[8] = {};
     double *macro = nullptr;      // rho|ux|uy|uz ghosted
     double *scratch = nullptr;    // statistics partial sums / moments partials
     size_t scratch_bytes = 0;
@@ -287,10 +287,28 @@ int build_mesh(dg_ctx *h)
 // ---------------------------------------------------------------------------
 // parameter blocks
 // ---------------------------------------------------------------------------
-// T-typed tables (x-face normal weights, transverse x weights, dt/dxx, perturbation factors)
+// Uniform lerp weights of the y and z directions, in the reference's real R:
+// transverse |hdt/dy|, |hdt/dz| (src/dugks.cu:769-770) and the y / z face
+// normal fractions (dy/2 - hdt c_y)/dy, (dz/2 - hdt c_z)/dz (828, 871).
+template <class R>
+struct YZWeights {
+    R ty, tz, yn[19], zn[19];
+    explicit YZWeights(const RefCoef<R> &c)
+    {
+        ty = std::fabs((-c.hdt * 1) / c.dy);
+        tz = std::fabs((-c.hdt * 1) / c.dz);
+        for (int p = 0; p < 19; ++p) {
+            yn[p] = (c.dy / 2. - c.hdt * dg::cy(p)) / c.dy;
+            zn[p] = (c.dz / 2. - c.hdt * dg::cz(p)) / c.dz;
+        }
+    }
+};
+
+// T-typed tables (x-face normal weights, transverse x weights, corner weights,
+// dt/dxx, perturbation factors)
 template <class T, class R>
 void make_tables(const dg_ctx *h, const RefCoef<R> &c, std::vector<T> &xw, std::vector<T> &txw, std::vector<T> &cxu,
-                 std::vector<T> &px, std::vector<T> &py, std::vector<T> &pz, std::vector<T> &cxuf)
+                 std::vector<T> &px, std::vector<T> &py, std::vector<T> &pz, std::vector<T> &cxuf, std::vector<T> &cw)
 {
     const int nx = h->nx, ny = h->ny, nz = h->nz;
     const bool st = h->mesh != 0;
@@ -330,6 +348,59 @@ void make_tables(const dg_ctx *h, const RefCoef<R> &c, std::vector<T> &xw, std::
                     t = std::fabs((-hdt * cxp) / (R(0.5) * R(h->dxx[gi]) + R(0.5) * R(h->dxx[gi - cxp])));  // dugks.cuf:595
                 txw[size_t(2 * p) * xs + gi] = T(R(1 - t));
                 txw[size_t(2 * p + 1) * xs + gi] = T(t);
+            }
+        }
+    }
+    // corner weights: products of the lerp weights as T values, evaluated in
+    // double (exact for the FP32 tables' float factors)
+    cw.assign(xs * dg::CW_ROWS, T(0));
+    {
+        const YZWeights<R> yz(c);
+        const double tyo = double(T(R(1 - yz.ty))), tym = double(T(yz.ty));
+        const double tzo = double(T(R(1 - yz.tz))), tzm = double(T(yz.tz));
+        auto put = [&](int row, int col, double w) { cw[size_t(row) * xs + col] = T(w); };
+        for (int I = 0; I <= nx; ++I) {
+            for (int cl = 1; cl <= 3; ++cl) {
+                const double om = double(xw[size_t(2 * cl) * xs + I]), m = double(xw[size_t(2 * cl + 1) * xs + I]);
+                const int y = dg::CW_XY + 4 * (cl - 1), z = dg::CW_XZ + 4 * (cl - 1);
+                put(y, I, tyo * om); put(y + 1, I, tyo * m); put(y + 2, I, tym * om); put(y + 3, I, tym * m);
+                put(z, I, tzo * om); put(z + 1, I, tzo * m); put(z + 2, I, tzm * om); put(z + 3, I, tzm * m);
+                if (cl == 3) {
+                    const double a[4] = {tzo * tyo, tzo * tym, tzm * tyo, tzm * tym};
+                    for (int q = 0; q < 4; ++q) {
+                        put(dg::CW_XYZ + 2 * q, I, a[q] * om);
+                        put(dg::CW_XYZ + 2 * q + 1, I, a[q] * m);
+                    }
+                }
+            }
+        }
+        for (int gi = 1; gi <= nx; ++gi) {
+            for (int p = 1; p < 19; ++p) {
+                if (dg::cx(p) == 0) continue;
+                const int cl = dg::xrep(p);
+                const double txo = double(txw[size_t(2 * cl) * xs + gi]), txm = double(txw[size_t(2 * cl + 1) * xs + gi]);
+                const double yo = double(T(R(1 - yz.yn[p]))), ym = double(T(yz.yn[p]));
+                const double zo = double(T(R(1 - yz.zn[p]))), zm = double(T(yz.zn[p]));
+                if (dg::cz(p) == 0) {  // y face, 4 corners (rows A, B x columns i, i - cx)
+                    const int r = dg::CW_Y4 + 4 * dg::slot4y(p);
+                    put(r, gi, yo * txo); put(r + 1, gi, yo * txm); put(r + 2, gi, ym * txo); put(r + 3, gi, ym * txm);
+                } else {               // y face, 8 corners (c_y = 0): planes k, k - cz
+                    const int r = dg::CW_Y8 + 8 * (cl - 1);
+                    put(r, gi, tzo * yo * txo); put(r + 1, gi, tzo * yo * txm);
+                    put(r + 2, gi, tzo * ym * txo); put(r + 3, gi, tzo * ym * txm);
+                    put(r + 4, gi, tzm * yo * txo); put(r + 5, gi, tzm * yo * txm);
+                    put(r + 6, gi, tzm * ym * txo); put(r + 7, gi, tzm * ym * txm);
+                }
+                if (dg::cy(p) == 0) {  // z face, 4 corners (planes A, B x columns i, i - cx)
+                    const int r = dg::CW_Z4 + 4 * dg::slot4z(p);
+                    put(r, gi, zo * txo); put(r + 1, gi, zo * txm); put(r + 2, gi, zm * txo); put(r + 3, gi, zm * txm);
+                } else {               // z face, 8 corners (c_z = 0): rows j, j - cy
+                    const int r = dg::CW_Z8 + 8 * (cl - 1);
+                    put(r, gi, zo * tyo * txo); put(r + 1, gi, zo * tyo * txm);
+                    put(r + 2, gi, zo * tym * txo); put(r + 3, gi, zo * tym * txm);
+                    put(r + 4, gi, zm * tyo * txo); put(r + 5, gi, zm * tyo * txm);
+                    put(r + 6, gi, zm * tym * txo); put(r + 7, gi, zm * tym * txm);
+                }
             }
         }
     }
@@ -381,20 +452,33 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
         P.F[a] = T(c.F[a]);
         P.hF[a] = T(R(0.5 * c.hdt) * c.F[a]);  // 0.5*p->hdt*hp->ambient_f (src/dugks.cu:698)
     }
+    const YZWeights<R> yz(c);
     for (int p = 0; p < 19; ++p) {
         const R cf = R(dg::cx(p)) * c.F[0] + R(dg::cy(p)) * c.F[1] + R(dg::cz(p)) * c.F[2];
         P.Kb[p] = T(R(3) * c.bw0 * cf);
         P.Kf[p] = T(R(3) * c.fw0 * cf);
-        const R my1 = (c.dy / 2. - c.hdt * dg::cy(p)) / c.dy;  // src/dugks.cu:828
-        const R mz1 = (c.dz / 2. - c.hdt * dg::cz(p)) / c.dz;  // src/dugks.cu:871
-        P.yn_m[p] = T(my1); P.yn_om[p] = T(R(1 - my1));
-        P.zn_m[p] = T(mz1); P.zn_om[p] = T(R(1 - mz1));
+        P.yn_m[p] = T(yz.yn[p]); P.yn_om[p] = T(R(1 - yz.yn[p]));
+        P.zn_m[p] = T(yz.zn[p]); P.zn_om[p] = T(R(1 - yz.zn[p]));
     }
-    const R ty = std::fabs((-c.hdt * 1) / c.dy), tz = std::fabs((-c.hdt * 1) / c.dz);  // src/dugks.cu:769-770
-    P.ty_m = T(ty); P.ty_om = T(R(1 - ty));
-    P.tz_m = T(tz); P.tz_om = T(R(1 - tz));
+    P.ty_m = T(yz.ty); P.ty_om = T(R(1 - yz.ty));
+    P.tz_m = T(yz.tz); P.tz_om = T(R(1 - yz.tz));
+    // uniform corner weights of the y faces with c_x = 0 != c_z (rows j, j+1 at
+    // planes k, k - cz) and of the z faces with c_x = 0 != c_y (planes k, k+1 at
+    // rows j, j - cy), for face_tri_cw
+    for (int p = 1; p < 19; ++p) {
+        if (dg::cx(p) != 0) continue;
+        const double yo = double(P.yn_om[p]), ym = double(P.yn_m[p]), zo = double(P.zn_om[p]), zm = double(P.zn_m[p]);
+        const double tyo = double(P.ty_om), tym = double(P.ty_m), tzo = double(P.tz_om), tzm = double(P.tz_m);
+        if (dg::cz(p) != 0) {
+            P.ycw[p][0] = T(tzo * yo); P.ycw[p][1] = T(tzo * ym); P.ycw[p][2] = T(tzm * yo); P.ycw[p][3] = T(tzm * ym);
+        }
+        if (dg::cy(p) != 0) {
+            P.zcw[p][0] = T(zo * tyo); P.zcw[p][1] = T(zo * tym); P.zcw[p][2] = T(zm * tyo); P.zcw[p][3] = T(zm * tym);
+        }
+    }
     P.cyu = T(c.dt / c.dy);
     P.czu = T(c.dt / c.dz);
+    P.bwF = T(c.bw2 * c.hdt + c.bw0);
     P.fw2s = T(c.fw2 / c.fw1);
     P.fw0x3s = T(R(3) * c.fw0 / c.fw1);
     for (int p = 0; p < 19; ++p) {
@@ -419,6 +503,7 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     P.txw = reinterpret_cast<const T *>(base + h->tab_off[1]);
     P.cxu = reinterpret_cast<const T *>(base + h->tab_off[2]);
     P.cxuf = reinterpret_cast<const T *>(base + h->tab_off[6]);
+    P.cw = reinterpret_cast<const T *>(base + h->tab_off[7]);
     P.err = h->dev_err;
     P.pert_x = reinterpret_cast<const T *>(base + h->tab_off[3]);
     P.pert_y = reinterpret_cast<const T *>(base + h->tab_off[4]);
@@ -723,19 +808,19 @@ int adjoint_form(dg_ctx *h, int istep, const void *f_n, const void *lam_next, vo
 template <class T>
 int upload_tables(dg_ctx *h)
 {
-    std::vector<T> xw, txw, cxu, px, py, pz, cxuf;
+    std::vector<T> xw, txw, cxu, px, py, pz, cxuf, cw;
     if (h->prec == DG_PREC_FP64)
-        make_tables<T, double>(h, h->c64, xw, txw, cxu, px, py, pz, cxuf);
+        make_tables<T, double>(h, h->c64, xw, txw, cxu, px, py, pz, cxuf, cw);
     else
-        make_tables<T, float>(h, h->c32, xw, txw, cxu, px, py, pz, cxuf);
-    const std::vector<T> *parts[7] = {&xw, &txw, &cxu, &px, &py, &pz, &cxuf};
+        make_tables<T, float>(h, h->c32, xw, txw, cxu, px, py, pz, cxuf, cw);
+    const std::vector<T> *parts[8] = {&xw, &txw, &cxu, &px, &py, &pz, &cxuf, &cw};
     size_t off = 0;
-    for (int t = 0; t < 7; ++t) {
+    for (int t = 0; t < 8; ++t) {
         h->tab_off[t] = off;
         off += (parts[t]->size() * sizeof(T) + 255) / 256 * 256;
     }
     CK(cudaMalloc(&h->tab, off), "cudaMalloc (tables)");
-    for (int t = 0; t < 7; ++t)
+    for (int t = 0; t < 8; ++t)
         CK(cudaMemcpy(static_cast<char *>(h->tab) + h->tab_off[t], parts[t]->data(), parts[t]->size() * sizeof(T),
                       cudaMemcpyHostToDevice),
            "table upload");

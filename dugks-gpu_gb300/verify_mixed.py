@@ -13,6 +13,13 @@ after `--burn` steps, and reports per form:
   MLUPS     step throughput of the form (device-resident, CUDA events)
   mass      relative drift of the volume-weighted mass
 
+The form `fp64p` is FP64 from the same start with every value multiplied by
+(1 + eps r), r uniform in [-1, 1) (seeded, eps = --pert): its errors against
+FP64 are the sampling floor of a chaotic flow, the difference that any change
+of rounding makes to finite-time averages once the trajectories have
+decorrelated; errors of the reduced forms at that level are not precision
+errors.
+
 Reference orientation: x wall-normal, y spanwise, z streamwise.
 
   python dugks-gpu_gb300/verify_mixed.py --steps 5000 --every 10 --burn 1000
@@ -30,11 +37,16 @@ sys.path.insert(0, HERE)
 import pydugks  # noqa: E402
 
 
-def run_form(prec, args):
+def run_form(form, args):
     import torch
+    prec = "fp64" if form == "fp64p" else form
     cfg, meta = pydugks.channel_config(nx=args.nx, ny=args.ny, nz=args.nz, precision=prec)
     eng = pydugks.Engine(cfg)
     eng.set_stream(torch.cuda.current_stream().cuda_stream)
+    if form == "fp64p":
+        f = eng.get_state()
+        r = np.random.default_rng(args.seed).uniform(-1.0, 1.0, f.shape)
+        eng.set_state(f * (1.0 + args.pert * r))
     _, dxx = eng.mesh()
     w = dxx[1:-1]
     m0 = float((eng.get_state().sum(axis=-1) * w).sum())
@@ -81,20 +93,46 @@ def main():
     ap.add_argument("--every", type=int, default=10)
     ap.add_argument("--burn", type=int, default=1000)
     ap.add_argument("--forms", default="fp64,fp32,fp16,bf16")
+    ap.add_argument("--pert", type=float, default=1e-12, help="relative perturbation of the fp64p start")
+    ap.add_argument("--seed", type=int, default=1, help="seed of the fp64p perturbation")
+    ap.add_argument("--save", default="", help="write the time-averaged profiles of every form to this .npz")
+    ap.add_argument("--ref", default="", help="take the FP64 (and fp64p) results from a --save file of the "
+                    "same workload instead of running them")
     args = ap.parse_args()
     forms = args.forms.split(",")
     t0 = time.time()
-    res = {p: run_form(p, args) for p in forms}
+    res = {}
+    if args.ref:
+        z = np.load(args.ref)
+        for p in ("fp64", "fp64p"):
+            if p in z.files:
+                get = lambda key, d: float(z[key]) if key in z.files else d  # noqa: E731
+                res[p] = dict(prof=z[p], count=int(get(p + "_count", 0)), mlups=get(p + "_mlups", float("nan")),
+                              mass_drift=get(p + "_mass", float("nan")), utau=float(z["utau"]))
+        forms = [p for p in ("fp64", "fp64p") if p in res] + [p for p in forms if p not in res]
+    for p in forms:
+        if p not in res:
+            res[p] = run_form(p, args)
     ref = res["fp64"]
     out = {"workload": f"channel Re_tau=180 {args.nz}x{args.nx}x{args.ny} (stream x wall x span), tanh mesh",
            "steps": args.steps, "burn": args.burn, "every": args.every, "samples": ref["count"],
            "wall_s": time.time() - t0, "forms": {}}
+    if "fp64p" in forms:
+        out["pert"] = args.pert
     for p in forms:
         r = res[p]
         d = {"mlups": r["mlups"], "mass_drift": r["mass_drift"], "speedup_vs_fp64": r["mlups"] / ref["mlups"]}
         if p != "fp64":
             d.update(errors(r["prof"], ref["prof"], ref["utau"]))
         out["forms"][p] = d
+    if args.save:
+        arrs = {}
+        for p in forms:
+            arrs[p] = np.asarray(res[p]["prof"])
+            arrs[p + "_count"] = res[p]["count"]
+            arrs[p + "_mlups"] = res[p]["mlups"]
+            arrs[p + "_mass"] = res[p]["mass_drift"]
+        np.savez(args.save, utau=ref["utau"], **arrs)
     print(json.dumps(out))
 
 
