@@ -48,11 +48,13 @@ constexpr int CW_ROWS = 112;
 __host__ __device__ constexpr int slot4y(int p) { return p == 1 ? 0 : (p == 2 ? 1 : p - 5); }
 __host__ __device__ constexpr int slot4z(int p) { return p == 1 ? 0 : (p == 2 ? 1 : p - 9); }
 
-// The corner-weight faces are used where the FP64 pipe bounds the step.
+// Forms whose throughput is set by the FP64 instruction count: they take the
+// corner-weight faces and the one-axis force paths, which trade FP64
+// operations for table loads and integer selects.
 template <class T>
-struct CornerWeights { static constexpr bool value = false; };
+struct Fp64Form { static constexpr bool value = false; };
 template <>
-struct CornerWeights<double> { static constexpr bool value = true; };
+struct Fp64Form<double> { static constexpr bool value = true; };
 
 template <class T, class S>
 struct StepParams {
@@ -63,10 +65,12 @@ struct StepParams {
     int periodic_x;        // 0: bounce-back walls on the two x faces
     int perturb;           // per-cell perturbation force in stage (a)
     int force_on;          // ambient force non-zero
+    int fax;               // the axis of the ambient force if at most one component is non-zero, else -1
     // stage (a)
     T hdt, bw1, bw2, bw0x3;      // bw0x3 = 3*bw0
     T F[3];                      // ambient force
     T Kb[NPOP];                  // 3*bw0*(c_p . F)
+    T Fa, hFa, Kba, Kfa;         // fax >= 0: F, (0.5*hdt)*F, Kb, Kfs of the force axis (c_p = +1 on it)
     // faces
     T fw1, fw2, fw0x3;           // fw0x3 = 3*fw0
     T hF[3];                     // (0.5*hdt)*F, the face velocity shift (src/dugks.cu:698-700)
@@ -299,14 +303,26 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     T Fx, Fy, Fz;
     cell_force(P, ic, j, k, Fx, Fy, Fz);
     const bool forced = P.force_on || P.perturb || P.ffield;
-    if (forced) {
+    // one ambient force component and no per-cell force: the same values from
+    // that component alone, and B + K_p in three values (FP64 form)
+    const bool one_axis = Fp64Form<T>::value && P.fax >= 0 && !P.perturb && !P.ffield;
+    // coefficient of feq: bw2 + 3 bw0 (F.c - F.u) = B + K_p
+    T B = P.bw2;
+    if (one_axis) {
+        if (P.force_on) {
+            const int a = P.fax;
+            const T ua = fma(P.hdt, P.Fa, a == 0 ? u : (a == 1 ? vv : w));
+            u = a == 0 ? ua : u;
+            vv = a == 1 ? ua : vv;
+            w = a == 2 ? ua : w;
+            B = fma(-P.bw0x3, P.Fa * ua, P.bw2);
+        }
+    } else if (forced) {
         u = fma(P.hdt, Fx, u);
         vv = fma(P.hdt, Fy, vv);
         w = fma(P.hdt, Fz, w);
+        B = fma(-P.bw0x3, fma(Fx, u, fma(Fy, vv, Fz * w)), P.bw2);
     }
-    // coefficient of feq: bw2 + 3 bw0 (F.c - F.u) = B + K_p
-    T B = P.bw2;
-    if (forced) B = fma(-P.bw0x3, fma(Fx, u, fma(Fy, vv, Fz * w)), P.bw2);
 
     T fe[NPOP];
     feq_all(r, u, vv, w, fe);
@@ -323,8 +339,18 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
         return fma(B + K, fe[p], P.bw1 * v[p]);
     };
     T ob[NPOP];
+    if (one_axis) {
+        const T Bp = B + P.Kba, Bm = B - P.Kba;
+        const int a = P.fax;
 #pragma unroll
-    for (int p = 0; p < NPOP; ++p) ob[p] = fbar_p(p);
+        for (int p = 0; p < NPOP; ++p) {
+            const int ca = a == 0 ? cx(p) : (a == 1 ? cy(p) : cz(p));
+            ob[p] = fma(ca > 0 ? Bp : (ca < 0 ? Bm : B), fe[p], P.bw1 * v[p]);
+        }
+    } else {
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) ob[p] = fbar_p(p);
+    }
     if (sizeof(T) == 4) {
         // FP32 arithmetic: the moments of f-bar-plus are set to their exact values
         // (exact arithmetic: sum f-bar-plus = rho, sum c f-bar-plus = j + rho F
@@ -830,6 +856,14 @@ __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[N
         vv = fma(hh, Ff[1], vv);
         w = fma(hh, Ff[2], w);
         B = fma(-P.fw0x3s, fma(Ff[0], u, fma(Ff[1], vv, Ff[2] * w)), P.fw2s);
+    } else if (Fp64Form<T>::value && P.force_on && P.fax >= 0) {
+        // one force component: the same values from that component alone
+        const int a = P.fax;
+        const T ua = (a == 0 ? u : (a == 1 ? vv : w)) + P.hFa;
+        u = a == 0 ? ua : u;
+        vv = a == 1 ? ua : vv;
+        w = a == 2 ? ua : w;
+        B = fma(-P.fw0x3s, P.Fa * ua, P.fw2s);
     } else if (P.force_on) {
         u += P.hF[0];
         vv += P.hF[1];
@@ -858,6 +892,18 @@ __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[N
     if (AX != 0) {
         feq_pair(v3 + w3, base, wr2, fe[15], fe[18]);
         feq_pair(w3 - v3, base, wr2, fe[16], fe[17]);
+    }
+    if (Fp64Form<T>::value && !FF && P.fax >= 0) {
+        // B + K_p takes three values: B, B + Kfa, B - Kfa
+        const T Bp = B + P.Kfa, Bm = B - P.Kfa;
+        const int a = P.fax;
+#pragma unroll
+        for (int s = 0; s < 10; ++s) {
+            const int p = flux_pop(AX, s);
+            const int ca = a == 0 ? cx(p) : (a == 1 ? cy(p) : cz(p));
+            out[s] = fma(ca > 0 ? Bp : (ca < 0 ? Bm : B), fe[p], v[p]);
+        }
+        return;
     }
 #pragma unroll
     for (int s = 0; s < 10; ++s) {
@@ -912,7 +958,7 @@ template <class T, class S, int AX, int RECON, bool FF, class RD>
 __device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const RD &R, int i, int j, int k, T out[10])
 {
     T v[NPOP];
-    if (RECON == 0 && CornerWeights<T>::value)
+    if (RECON == 0 && Fp64Form<T>::value)
         face_tri_cw<T, S, AX>(P, R, i, j, k, v);
     else if (RECON == 0)
         face_tri<T, S, AX>(P, R, i, j, k, v);

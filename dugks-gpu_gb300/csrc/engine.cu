@@ -446,6 +446,10 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     P.periodic_x = h->periodic[0];
     P.perturb = h->perturb;
     P.force_on = (c.F[0] != 0 || c.F[1] != 0 || c.F[2] != 0) ? 1 : 0;
+    {
+        const int nnz = (c.F[0] != 0) + (c.F[1] != 0) + (c.F[2] != 0);
+        P.fax = nnz > 1 ? -1 : (c.F[1] != 0 ? 1 : (c.F[2] != 0 ? 2 : 0));
+    }
     P.hdt = T(c.hdt); P.bw1 = T(c.bw1); P.bw2 = T(c.bw2); P.bw0x3 = T(R(3) * c.bw0);
     P.fw1 = T(c.fw1); P.fw2 = T(c.fw2); P.fw0x3 = T(R(3) * c.fw0);
     for (int a = 0; a < 3; ++a) {
@@ -479,6 +483,14 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     P.cyu = T(c.dt / c.dy);
     P.czu = T(c.dt / c.dz);
     P.bwF = T(c.bw2 * c.hdt + c.bw0);
+    if (P.fax >= 0) {
+        // the values of the tables at a population with c = +1 on the force axis
+        const R Fa = c.F[P.fax];
+        P.Fa = T(Fa);
+        P.hFa = T(R(0.5 * c.hdt) * Fa);
+        P.Kba = T(R(3) * c.bw0 * Fa);
+        P.Kfa = T(R(3) * c.fw0 * Fa / c.fw1);
+    }
     P.fw2s = T(c.fw2 / c.fw1);
     P.fw0x3s = T(R(3) * c.fw0 / c.fw1);
     for (int p = 0; p < 19; ++p) {
