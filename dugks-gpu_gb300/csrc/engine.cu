@@ -110,7 +110,7 @@ struct dg_ctx {
     int prec = DG_PREC_FP64;
     int mesh = 0;           // 0 uniform, 1 tanh, 2 file
     int recon = 0;          // 0 trilinear
-    int stochastic = 1;     // BF16 form: stochastic rounding of the stored deviations
+    int stochastic = 1;     // 16-bit forms: stochastic rounding of the stored deviations
     double mesh_alpha = 0.85;
     std::string mesh_file;
     // derived
@@ -540,11 +540,16 @@ void set_codec<float, __nv_bfloat16>(const dg_ctx *h, Codec<float, __nv_bfloat16
     }
 }
 
-// per-step stochastic-rounding seed of the BF16 form (other forms: nothing)
+// per-step stochastic-rounding seed of the 16-bit forms (other forms: nothing)
 template <class T, class S>
 void set_round_seed(const dg_ctx *, Codec<T, S> &, int) {}
 template <>
 void set_round_seed<float, __nv_bfloat16>(const dg_ctx *h, Codec<float, __nv_bfloat16> &c, int istep)
+{
+    c.sr_seed = h->stochastic ? (mix32(unsigned(istep)) | 1u) : 0u;
+}
+template <>
+void set_round_seed<float, __half>(const dg_ctx *h, Codec<float, __half> &c, int istep)
 {
     c.sr_seed = h->stochastic ? (mix32(unsigned(istep)) | 1u) : 0u;
 }
@@ -591,7 +596,7 @@ template <class T, class S>
 bool graph_eligible(const dg_ctx *h)
 {
     if (h->perturb) return false;
-    if (std::is_same<S, __nv_bfloat16>::value && h->stochastic) return false;
+    if ((std::is_same<S, __nv_bfloat16>::value || std::is_same<S, __half>::value) && h->stochastic) return false;
     return true;
 }
 

@@ -4,11 +4,12 @@
 //   Codec<float, __half>, Codec<float, __nv_bfloat16>: 16-bit deviations from
 //       the rest-state equilibrium, d_p = (f_p - w_p) / s_p, with one scale s_p
 //       per population; decoded and re-encoded in FP32 (the mixed form).
-//       BF16 (8 significant bits) is written with stochastic rounding when
-//       sr_seed != 0: 16 hashed bits of (index, population, seed) are added
-//       below the BF16 mantissa before truncation, so the rounding error has
-//       zero mean and does not bias time averages; the seed changes every
-//       step and the result stays deterministic.  The step kernels hash the
+//       Stochastic rounding when sr_seed != 0 (the default of both forms;
+//       config key rounding=nearest turns it off): hashed bits of (index, population, seed) are added below
+//       the 16-bit mantissa of the float deviation before truncation (16 bits
+//       for BF16, 13 for FP16), so the rounding error has zero mean and does
+//       not bias time averages; the seed changes every step and the result
+//       stays deterministic.  The step kernels hash the
 //       cell once (cell_hash) and draw the population's bits from it with one
 //       multiply by an odd constant (store_h), a bijection of the hash, so
 //       each population's bits stay uniformly distributed.
@@ -41,7 +42,7 @@ struct DevCodec {
     float w[NPOP];    // rest-state equilibrium w_p (feq(rho=1, u=0))
     float s[NPOP];    // scale s_p
     float is[NPOP];   // 1 / s_p
-    unsigned sr_seed; // BF16: 0 round to nearest, else stochastic rounding with this seed
+    unsigned sr_seed; // 0: round to nearest, else stochastic rounding with this seed
     static constexpr bool deviation = true;
 };
 
@@ -70,18 +71,39 @@ struct Codec<float, __half> : DevCodec<__half> {
     {
         return fmaf(s[p], __half2float(a[idx]), w[p]);
     }
+    // FP16 keeps 10 of the float's 23 fraction bits: r (13 random bits) added
+    // to the float's bit pattern carries into the kept bits with probability
+    // equal to the dropped fraction; the truncated float is then exact in FP16
+    // (normal range; below 2^-14 the conversion truncates further, an error
+    // under 2^-24 in deviation units).
+    static __device__ __forceinline__ __half sr_half(float d, unsigned r)
+    {
+        const float t = __uint_as_float((__float_as_uint(d) + r) & ~0x1fffu);
+        return __float2half_rz(t);
+    }
     __device__ __forceinline__ void store(__half *a, long long idx, int p, float v) const
     {
-        a[idx] = __float2half_rn((v - w[p]) * is[p]);
+        const float d = (v - w[p]) * is[p];
+        if (sr_seed == 0) {
+            a[idx] = __float2half_rn(d);
+            return;
+        }
+        const unsigned r = mix32(unsigned(idx) * 19u + unsigned(p) + sr_seed * 0x9e3779b9u);
+        a[idx] = sr_half(d, r & 0x1fffu);
     }
-    __device__ __forceinline__ unsigned cell_hash(long long) const { return 0u; }
-    __device__ __forceinline__ __half encode_h(int p, float v, unsigned) const
+    __device__ __forceinline__ unsigned cell_hash(long long cell) const
     {
-        return __float2half_rn((v - w[p]) * is[p]);
+        return sr_seed ? (mix32(unsigned(cell) ^ sr_seed) | 1u) : 0u;
     }
-    __device__ __forceinline__ void store_h(__half *a, long long idx, int p, float v, unsigned) const
+    __device__ __forceinline__ __half encode_h(int p, float v, unsigned h) const
     {
-        store(a, idx, p, v);
+        const float d = (v - w[p]) * is[p];
+        if (h == 0u) return __float2half_rn(d);
+        return sr_half(d, (h * (0x9e3779b1u + 0x6a09e66eu * unsigned(p))) >> 19);  // odd multiplier per p
+    }
+    __device__ __forceinline__ void store_h(__half *a, long long idx, int p, float v, unsigned h) const
+    {
+        a[idx] = encode_h(p, v, h);
     }
     __device__ __forceinline__ float raw_nc(const __half *a, long long idx) const { return __half2float(__ldg(a + idx)); }
     __device__ __forceinline__ float raw_s(const __half *a, int idx) const { return __half2float(a[idx]); }

@@ -18,7 +18,8 @@ The form `fp64p` is FP64 from the same start with every value multiplied by
 FP64 are the sampling floor of a chaotic flow, the difference that any change
 of rounding makes to finite-time averages once the trajectories have
 decorrelated; errors of the reduced forms at that level are not precision
-errors.  `bf16n` is the BF16 form with round-to-nearest storage.
+errors.  `bf16n` is the BF16 form with round-to-nearest storage, `fp16s` the
+FP16 form with stochastic rounding.
 
 Reference orientation: x wall-normal, y spanwise, z streamwise.
 
@@ -39,8 +40,8 @@ import pydugks  # noqa: E402
 
 def run_form(form, args):
     import torch
-    prec = {"fp64p": "fp64", "bf16n": "bf16"}.get(form, form)
-    extra = {"rounding": "nearest"} if form == "bf16n" else {}
+    prec = {"fp64p": "fp64", "bf16n": "bf16", "fp16s": "fp16"}.get(form, form)
+    extra = {"bf16n": {"rounding": "nearest"}, "fp16s": {"rounding": "stochastic"}}.get(form, {})
     cfg, meta = pydugks.channel_config(nx=args.nx, ny=args.ny, nz=args.nz, precision=prec, **extra)
     eng = pydugks.Engine(cfg)
     eng.set_stream(torch.cuda.current_stream().cuda_stream)

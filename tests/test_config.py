@@ -85,6 +85,8 @@ def test_bad_extension_values():
     assert create(pydugks.make_config(mesh="tanh", periods_x=1))[0] == DG_ERR_CONFIG
     assert create(pydugks.make_config(precision="bf16", rounding="up"))[0] == DG_ERR_CONFIG
     assert gpu_or_ok(create(pydugks.make_config(precision="bf16", rounding="nearest"))[0])
+    assert create(pydugks.make_config(precision="fp16", rounding="down"))[0] == DG_ERR_CONFIG
+    assert gpu_or_ok(create(pydugks.make_config(precision="fp16", rounding="stochastic"))[0])
 
 
 def test_tiny_grid_rejected():

@@ -3,10 +3,10 @@ FP32 arithmetic) against the FP64 oracle.
 
 Bounds: after 10 steps from a seeded state the max-norm error relative to the
 oracle stays within 3 storage quanta of the largest deviation from the rest
-equilibrium (quantum 2^-11 for FP16, 2^-8 for BF16; measured 0.1-0.8 quanta);
-the total mass drifts by less than a tenth of a quantum over 200 steps; runs
-are deterministic (stochastic rounding included, its seed is the step
-number).
+equilibrium (quantum 2^-11 for FP16, 2^-8 for BF16; measured 0.1-0.8 quanta)
+with either rounding of either form; the total mass drifts by less than a
+tenth of a quantum over 200 steps; runs are deterministic (stochastic
+rounding included, its seed is the step number).
 """
 import numpy as np
 import pytest
@@ -24,7 +24,8 @@ def _maxdev(f0):
     return float(np.max(np.abs(f0 - w) / w))
 
 
-@pytest.mark.parametrize("prec,rounding", [("fp16", "stochastic"), ("bf16", "stochastic"), ("bf16", "nearest")])
+@pytest.mark.parametrize("prec,rounding", [("fp16", "stochastic"), ("fp16", "nearest"), ("bf16", "stochastic"),
+                                           ("bf16", "nearest")])
 @pytest.mark.parametrize("case", ["walls", "periodic", "stretched"])
 def test_16bit_forms_stay_within_the_storage_quantum(case, prec, rounding):
     n = 10
@@ -50,10 +51,11 @@ def test_16bit_mass_drift(prec):
     assert drift < 0.1 * QUANT[prec] * max(1e-3, _maxdev(f0))
 
 
-def test_bf16_runs_are_deterministic_and_rounding_modes_differ():
+@pytest.mark.parametrize("prec", ["bf16", "fp16"])
+def test_16bit_runs_are_deterministic_and_rounding_modes_differ(prec):
     outs = []
     for rounding in ("stochastic", "stochastic", "nearest"):
-        eng, _, _ = make_pair("walls", precision="bf16", rounding=rounding)
+        eng, _, _ = make_pair("walls", precision=prec, rounding=rounding)
         eng.run(1, 15)
         outs.append(eng.get_state())
         eng.close()
