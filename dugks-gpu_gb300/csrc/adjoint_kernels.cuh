@@ -23,25 +23,73 @@
 
 namespace dg {
 
+// Accumulators of S0 and G over the populations, without multiplications by
+// zero velocity components:
+//   S0 = sum lam_p coef_p feq_p,  Lf = sum lam_p feq_p,
+//   A = sum a_p,  Bd_d = sum a_p b_p c_pd   (a_p = lam_p coef_p w_p r, b_p = 3 + 9 c_p.u)
+// so that G_d = Bd_d - 3 u_d A - 3 w0 F_d Lf.
 template <class T>
 struct AdjJac {
-    T S0, G[3];
+    T S0, Lf, A, Bd[3];
 };
 
-// Accumulate one population's term of S0 and G; lam is the adjoint of
-// out_p = w1 x_p + coef_p feq_p with coef_p = cb + Kp (cb = w2 - 3 w0 F.u).
+// c_p . u from the non-zero components only
 template <class T>
-__device__ __forceinline__ void adj_accum(AdjJac<T> &J, int p, T lam, T r, T u, T v, T w, T coef, T feq,
-                                          T w0x3, const T F[3])
+__device__ __forceinline__ T cdot(int p, T u, T v, T w)
 {
-    const T cu = T(cx(p)) * u + T(cy(p)) * v + T(cz(p)) * w;
-    const T a = lam * coef * weight<T>(p) * r;
-    const T b = T(3) + T(9) * cu;
-    J.S0 += lam * coef * feq;
-    const T lf = lam * feq * w0x3;
-    J.G[0] += a * (b * T(cx(p)) - T(3) * u) - lf * F[0];
-    J.G[1] += a * (b * T(cy(p)) - T(3) * v) - lf * F[1];
-    J.G[2] += a * (b * T(cz(p)) - T(3) * w) - lf * F[2];
+    T s = T(0);
+    bool any = false;
+    if (cx(p)) { s = cx(p) > 0 ? u : -u; any = true; }
+    if (cy(p)) { s = any ? (cy(p) > 0 ? s + v : s - v) : (cy(p) > 0 ? v : -v); any = true; }
+    if (cz(p)) s = any ? (cz(p) > 0 ? s + w : s - w) : (cz(p) > 0 ? w : -w);
+    return s;
+}
+
+// One population's terms; lam is the adjoint of out_p = w1 x_p + coef_p feq_p
+// and wr = w_p r.
+template <class T>
+__device__ __forceinline__ void adj_accum(AdjJac<T> &J, int p, T lam, T wr, T u, T v, T w, T coef, T feq)
+{
+    const T lc = lam * coef;
+    J.S0 = fma(lc, feq, J.S0);
+    J.Lf = fma(lam, feq, J.Lf);
+    const T a = lc * wr;
+    J.A += a;
+    const T b = fma(T(9), cdot(p, u, v, w), T(3));
+    if (cx(p)) J.Bd[0] = fma(cx(p) > 0 ? a : -a, b, J.Bd[0]);
+    if (cy(p)) J.Bd[1] = fma(cy(p) > 0 ? a : -a, b, J.Bd[1]);
+    if (cz(p)) J.Bd[2] = fma(cz(p) > 0 ? a : -a, b, J.Bd[2]);
+}
+
+// G without the force term (Gq_d = Bd_d - 3 u_d A) and with it (G_d = Gq_d - w0x3 F_d Lf)
+template <class T>
+__device__ __forceinline__ void adj_G(const AdjJac<T> &J, T u, T v, T w, T w0x3, const T F[3], T Gq[3], T G[3])
+{
+    Gq[0] = fma(T(-3) * u, J.A, J.Bd[0]);
+    Gq[1] = fma(T(-3) * v, J.A, J.Bd[1]);
+    Gq[2] = fma(T(-3) * w, J.A, J.Bd[2]);
+    const T fl = w0x3 * J.Lf;
+    G[0] = fma(-fl, F[0], Gq[0]);
+    G[1] = fma(-fl, F[1], Gq[1]);
+    G[2] = fma(-fl, F[2], Gq[2]);
+}
+
+// g_p = S0 + G.(c_p - u0) as K0 + G.c_p with K0 = S0 - G.u0
+template <class T>
+__device__ __forceinline__ T adj_g(int p, T K0, const T G[3])
+{
+    T g = K0;
+    if (cx(p)) g = cx(p) > 0 ? g + G[0] : g - G[0];
+    if (cy(p)) g = cy(p) > 0 ? g + G[1] : g - G[1];
+    if (cz(p)) g = cz(p) > 0 ? g + G[2] : g - G[2];
+    return g;
+}
+
+// w_p r of population p from the three class values
+template <class T>
+__device__ __forceinline__ T wr_of(int p, T wr0, T wr1, T wr2)
+{
+    return p == 0 ? wr0 : (p <= 6 ? wr1 : wr2);
 }
 
 template <class T, class S>
@@ -82,7 +130,10 @@ __device__ __forceinline__ void adj_face_values(const StepParams<T, S> &P, const
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const int I = AX == 0 ? F : 0, i = AX == 0 ? 1 : F;
     T v[NPOP];
-    face_tri<T, S, AX>(P, R, F, j, k, v);
+    if (Fp64Form<T>::value)
+        face_tri_cw<T, S, AX>(P, R, F, j, k, v);  // the forward's own face values
+    else
+        face_tri<T, S, AX>(P, R, F, j, k, v);
     const bool lo = AX == 0 && !P.periodic_x && I == 0;
     const bool hi = AX == 0 && !P.periodic_x && I == nx;
     bounce_back(v, lo, hi);
@@ -143,40 +194,38 @@ __device__ __forceinline__ void adj_face_values(const StepParams<T, S> &P, const
     }
     T fe[NPOP];
     feq_face<T, AX>(r, u, vv, w, fe);
-    AdjJac<T> Jc = {T(0), {T(0), T(0), T(0)}};
-    // with a field: L0 = sum lamF_p feq_p and L1 = sum lamF_p c_{a,p} feq_p along the field axis a
+    AdjJac<T> Jc = {T(0), T(0), T(0), {T(0), T(0), T(0)}};
+    // with a field: L1 = sum lamF_p c_{a,p} feq_p along the field axis a (Jc.Lf = sum lamF_p feq_p)
     const int fax = P.ffaxis;
-    T L0 = T(0), L1 = T(0);
+    const T wr1 = weight<T>(1) * r, wr2 = weight<T>(7) * r;
+    T L1 = T(0);
 #pragma unroll
     for (int s = 0; s < 10; ++s) {
         const int p = flux_pop(AX, s);
-        const T cfp = T(cx(p)) * Ff[0] + T(cy(p)) * Ff[1] + T(cz(p)) * Ff[2];
-        const T coef = B + P.fw0x3 * cfp;
-        adj_accum(Jc, p, lamF[p], r, u, vv, w, coef, fe[p], P.fw0x3, Ff);
+        // coef_p = fw2 + 3 fw0 (F.c_p - F.u): the table value without a field
+        const T coef = P.ffield ? fma(P.fw0x3, cdot(p, Ff[0], Ff[1], Ff[2]), B) : B + P.Kf[p];
+        adj_accum(Jc, p, lamF[p], wr_of(p, wr1, wr1, wr2), u, vv, w, coef, fe[p]);
         if (P.ffield) {
-            const T mf = lamF[p] * fe[p];
-            L0 += mf;
             const int ca = fax == 0 ? cx(p) : (fax == 1 ? cy(p) : cz(p));
-            if (ca) L1 += ca > 0 ? mf : -mf;
+            if (ca) L1 = fma(ca > 0 ? lamF[p] : -lamF[p], fe[p], L1);
         }
     }
+    T Gq[3], G[3];
+    adj_G(Jc, u, vv, w, P.fw0x3, Ff, Gq, G);
     if (P.ffield) {
         // dJ/dF_a = 3 fw0 sum lamF (c_a - u_a - hh F_a) feq + hh sum lamF coef d feq / d u_a
-        //         = 3 fw0 (L1 - (u_a + hh F_a) L0) + hh (Jc.G[a] + 3 fw0 F_a L0)
+        //         = 3 fw0 (L1 - (u_a + hh F_a) Lf) + hh Gq_a
         const T ua = fax == 0 ? u : (fax == 1 ? vv : w);
         const T Fa = fax == 0 ? Ff[0] : (fax == 1 ? Ff[1] : Ff[2]);
-        const T Ga = fax == 0 ? Jc.G[0] : (fax == 1 ? Jc.G[1] : Jc.G[2]);
-        const T Sc = L1 - (ua + hh * Fa) * L0;
-        const T Gq = Ga + P.fw0x3 * Fa * L0;
-        lf = P.fw0x3 * Sc + hh * Gq;
+        const T Gqa = fax == 0 ? Gq[0] : (fax == 1 ? Gq[1] : Gq[2]);
+        const T Sc = L1 - (ua + hh * Fa) * Jc.Lf;
+        lf = P.fw0x3 * Sc + hh * Gqa;
     } else {
         lf = T(0);
     }
+    const T K0 = fma(-G[2], w0, fma(-G[1], v0, fma(-G[0], u0, Jc.S0)));
 #pragma unroll
-    for (int p = 0; p < NPOP; ++p) {
-        const T g = Jc.S0 + Jc.G[0] * (T(cx(p)) - u0) + Jc.G[1] * (T(cy(p)) - v0) + Jc.G[2] * (T(cz(p)) - w0);
-        lv[p] = P.fw1 * lamF[p] + g * inv;
-    }
+    for (int p = 0; p < NPOP; ++p) lv[p] = fma(P.fw1, lamF[p], adj_g(p, K0, G) * inv);
     // bounce-back transpose
     if (lo) {
         lv[2] += lv[1]; lv[1] = T(0); lv[10] += lv[7]; lv[7] = T(0); lv[8] += lv[9]; lv[9] = T(0);
@@ -507,8 +556,8 @@ __global__ void __launch_bounds__(128, 12) adj_stencil_kernel(const T *__restric
                                                              T *__restrict__ MU, const StepParams<T, S> P)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y + 1, k = blockIdx.z / 4 + 1, grp = blockIdx.z % 4;
-    if (i > P.nx) return;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1, k = blockIdx.z / 4 + 1, grp = blockIdx.z % 4;
+    if (i > P.nx || j > P.ny) return;
     const AdjRows R = adj_rows(j, k, P.nx, P.ny, P.nz);
     const long long nfx = adj_nface(0, P.nx, P.ny, P.nz), nfc = adj_nface(1, P.nx, P.ny, P.nz);
     // second x face holding column i: face i-1 ("other" column), face 0 (anchor) at a wall,
@@ -542,8 +591,8 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
                                                          const T *__restrict__ MU, const StepParams<T, S> P)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y + 1, k = blockIdx.z + 1;
-    if (i > P.nx) return;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1, k = blockIdx.z + 1;
+    if (i > P.nx || j > P.ny) return;
     const long long c = ((long long)(k - 1) * P.ny + (j - 1)) * P.pitch + (i - 1);
     T mu[NPOP];
     {
@@ -572,10 +621,11 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
     }
     T fe[NPOP];
     feq_all(r, u, vv, w, fe);
-    AdjJac<T> Jc = {T(0), {T(0), T(0), T(0)}};
-    // with a field: L0 = sum mu_p feq_p and L1 = sum mu_p c_{a,p} feq_p along the field axis a
+    AdjJac<T> Jc = {T(0), T(0), T(0), {T(0), T(0), T(0)}};
+    // with a field: L1 = sum mu_p c_{a,p} feq_p along the field axis a (Jc.Lf = sum mu_p feq_p)
     const int fax = P.ffaxis;
-    T L0 = T(0), L1 = T(0);
+    const T wr0 = weight<T>(0) * r, wr1 = weight<T>(1) * r, wr2 = weight<T>(7) * r;
+    T L1 = T(0);
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
         T K = P.Kb[p];
@@ -586,31 +636,29 @@ __global__ void __launch_bounds__(128) adj_gather_kernel(const S *__restrict__ f
             if (cz(p)) cf += cz(p) > 0 ? Fz : -Fz;
             K = P.bw0x3 * cf;
         }
-        adj_accum(Jc, p, mu[p], r, u, vv, w, B + K, fe[p], P.bw0x3, Fc);
+        adj_accum(Jc, p, mu[p], wr_of(p, wr0, wr1, wr2), u, vv, w, B + K, fe[p]);
         if (P.ffield) {
-            const T mf = mu[p] * fe[p];
-            L0 += mf;
             const int ca = fax == 0 ? cx(p) : (fax == 1 ? cy(p) : cz(p));
-            if (ca) L1 += ca > 0 ? mf : -mf;
+            if (ca) L1 = fma(ca > 0 ? mu[p] : -mu[p], fe[p], L1);
         }
     }
+    T Gq[3], G[3];
+    adj_G(Jc, u, vv, w, P.bw0x3, Fc, Gq, G);
+    const T K0 = fma(-G[2], w0, fma(-G[1], v0, fma(-G[0], u0, Jc.S0)));
 #pragma unroll
     for (int p = 0; p < NPOP; ++p) {
-        const T g = Jc.S0 + Jc.G[0] * (T(cx(p)) - u0) + Jc.G[1] * (T(cy(p)) - v0) + Jc.G[2] * (T(cz(p)) - w0);
-        const T out = P.bw1 * mu[p] + g * inv - T(1.0 / 3.0) * T(lam_next[p * P.ps + c]);
+        const T out = P.bw1 * mu[p] + adj_g(p, K0, G) * inv - T(1.0 / 3.0) * T(lam_next[p * P.ps + c]);
         lam_out[p * P.ps + c] = S(out);
     }
     if (dphi && P.ffield) {
         // stage (a): d fb_p / dF_a = 3 bw0 (c_ap - u_a - hdt F_a) feq_p + coef_p hdt d feq_p / d u_a;
-        // summed with mu: Sc = L1 - (u_a + hdt F_a) L0 and, since Jc.G[a] holds the second
-        // sum minus 3 bw0 F_a L0, Gq = Jc.G[a] + 3 bw0 F_a L0
+        // summed with mu: Sc = L1 - (u_a + hdt F_a) Lf and the second sum Gq_a
         const T ua = fax == 0 ? u : (fax == 1 ? vv : w);
         const T Fa = fax == 0 ? Fx : (fax == 1 ? Fy : Fz);
-        const T Ga = fax == 0 ? Jc.G[0] : (fax == 1 ? Jc.G[1] : Jc.G[2]);
-        const T Sc = L1 - (ua + P.hdt * Fa) * L0;
-        const T Gq = Ga + P.bw0x3 * Fa * L0;
+        const T Gqa = fax == 0 ? Gq[0] : (fax == 1 ? Gq[1] : Gq[2]);
+        const T Sc = L1 - (ua + P.hdt * Fa) * Jc.Lf;
         // this step's contribution in the arithmetic type, accumulated over steps in FP64
-        T g = P.bw0x3 * Sc + P.hdt * Gq;
+        T g = P.bw0x3 * Sc + P.hdt * Gqa;
         // faces: the field enters each face through the mean over its two cells
         const int nx = P.nx, ny = P.ny, nz = P.nz;
         const int Il = P.periodic_x && i == 1 ? nx : i - 1;

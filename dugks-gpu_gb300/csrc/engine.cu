@@ -1456,6 +1456,36 @@ int dg_adjoint_step(dg_t *h, int istep, const void *f_n, const void *lam_next, v
     return DISPATCH(h, adjoint_form, istep, f_n, lam_next, lam_out);
 }
 
+int dg_run_store(dg_t *h, int istep0, int n, void *states, long long stride_bytes)
+{
+    if (!h || n < 0 || (n > 0 && !states)) return DG_ERR_ARG;
+    const long long sb = (long long)h->ps * 19 * (long long)storage_bytes(h->prec);
+    if (n > 1 && stride_bytes < sb) return h->fail(DG_ERR_ARG, "dg_run_store: stride smaller than one state");
+    char *base = static_cast<char *>(states);
+    for (int s = 0; s < n; ++s) {
+        if (base + s * stride_bytes == h->fb) return h->fail(DG_ERR_ARG, "dg_run_store: a state slot aliases f-bar-plus");
+        int rc = dg_get_state_device(h, base + s * stride_bytes);
+        if (!rc && s + 1 < n) rc = dg_step(h, istep0 + s);
+        if (rc) return rc;
+    }
+    return DG_OK;
+}
+
+int dg_adjoint_run(dg_t *h, int istep0, int n, const void *states, long long stride_bytes, void *lam)
+{
+    if (!h || n < 0 || (n > 0 && (!states || !lam))) return DG_ERR_ARG;
+    const long long sb = (long long)h->ps * 19 * (long long)storage_bytes(h->prec);
+    if (n > 1 && stride_bytes < sb) return h->fail(DG_ERR_ARG, "dg_adjoint_run: stride smaller than one state");
+    const char *base = static_cast<const char *>(states);
+    const char *lo = base, *hi = base + (n - 1) * stride_bytes + sb, *l = static_cast<const char *>(lam);
+    if (n > 0 && l + sb > lo && l < hi) return h->fail(DG_ERR_ARG, "dg_adjoint_run: lam overlaps the states");
+    for (int s = n - 1; s >= 0; --s) {
+        const int rc = dg_adjoint_step(h, istep0 + s, base + s * stride_bytes, lam, lam);
+        if (rc) return rc;
+    }
+    return DG_OK;
+}
+
 int dg_set_force_field(dg_t *h, int axis, const double *phi)
 {
     if (!h) return DG_ERR_ARG;

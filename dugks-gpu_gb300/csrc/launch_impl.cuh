@@ -214,9 +214,12 @@ cudaError_t Kern<T, S>::adjoint(const S *f_n, S *fb, const S *lam_next, S *lam_o
             adj_ghost_kernel<T, S><<<unsigned((ng + 31) / 32), 32, 0, st>>>(LX, LY, LZ, GH, P);
         }
         T *MU = GH + 2LL * NPOP * P.ny * P.nz;  // transposed-stencil sums, 19 * nx * ny * nz
-        dim3 grid((P.nx + 127) / 128, P.ny, P.nz);
-        adj_stencil_kernel<T, S><<<dim3(grid.x, grid.y, 4 * P.nz), 128, 0, st>>>(LX, LY, LZ, GH, MU, P);
-        adj_gather_kernel<T, S><<<grid, 128, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, LFX, LFY, LFZ, dphi, MU, P);
+        // 128-thread blocks of whole warps over x (one to four rows when nx < 128), so
+        // that narrow grids leave no lanes idle
+        const int bx = P.nx >= 128 ? 128 : (P.nx + 31) / 32 * 32, by = 128 / bx;
+        const dim3 blk(bx, by), grid((P.nx + bx - 1) / bx, (P.ny + by - 1) / by, P.nz);
+        adj_stencil_kernel<T, S><<<dim3(grid.x, grid.y, 4 * P.nz), blk, 0, st>>>(LX, LY, LZ, GH, MU, P);
+        adj_gather_kernel<T, S><<<grid, blk, 0, st>>>(f_n, lam_next, LX, LY, LZ, lam_out, LFX, LFY, LFZ, dphi, MU, P);
         return cudaGetLastError();
     }
 }

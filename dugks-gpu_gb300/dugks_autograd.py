@@ -92,19 +92,16 @@ class DugksRun(torch.autograd.Function):
         _sync_stream(eng)
         lam = lam_out.detach().contiguous().clone()
         nseg = (nsteps + every - 1) // every
+        # one buffer of `every` states, refilled per segment by the engine (recomputation and
+        # the reversed adjoint steps each run as one call)
+        states = torch.empty((min(every, nsteps), eng.soa_len), dtype=lam.dtype, device=lam.device)
+        stride = states.stride(0) * states.element_size()
         for seg in reversed(range(nseg)):
             s0, s1 = seg * every, min(nsteps, (seg + 1) * every)
             eng.set_state_device(ctx.cps[seg].data_ptr())
-            states = []
-            for s in range(s0, s1):
-                cur = empty_state(eng, lam.device)
-                eng.get_state_device(cur.data_ptr())
-                states.append(cur)
-                if s + 1 < s1:
-                    eng.step(istep0 + s)
-            for s in reversed(range(s0, s1)):
-                eng.adjoint_step(istep0 + s, states[s - s0].data_ptr(), lam.data_ptr(), lam.data_ptr())
-            del states
+            eng.run_store(istep0 + s0, s1 - s0, states.data_ptr(), stride)
+            eng.adjoint_run(istep0 + s0, s1 - s0, states.data_ptr(), stride, lam.data_ptr())
+        del states
         ctx.cps = None
         return lam, None, None, None, None
 

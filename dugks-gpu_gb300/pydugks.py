@@ -107,6 +107,9 @@ def lib():
         "dg_get_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
         "dg_set_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
         "dg_adjoint_step": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+        "dg_run_store": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong]),
+        "dg_adjoint_run": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_longlong,
+                                          ctypes.c_void_p]),
         "dg_set_force_field": (ctypes.c_int, [H, ctypes.c_int, _D]),
         "dg_field_grad": (ctypes.c_int, [H, _D, ctypes.c_int]),
     }
@@ -324,6 +327,13 @@ class Engine:
     def adjoint_step(self, istep, f_ptr, lam_next_ptr, lam_out_ptr):
         self._check(lib().dg_adjoint_step(self._h, istep, ctypes.c_void_p(f_ptr), ctypes.c_void_p(lam_next_ptr),
                                           ctypes.c_void_p(lam_out_ptr)))
+
+    def run_store(self, istep0, n, states_ptr, stride_bytes):
+        self._check(lib().dg_run_store(self._h, istep0, n, ctypes.c_void_p(states_ptr), stride_bytes))
+
+    def adjoint_run(self, istep0, n, states_ptr, stride_bytes, lam_ptr):
+        self._check(lib().dg_adjoint_run(self._h, istep0, n, ctypes.c_void_p(states_ptr), stride_bytes,
+                                         ctypes.c_void_p(lam_ptr)))
 
     def device_ptr(self, which):
         return lib().dg_device_ptr(self._h, which)

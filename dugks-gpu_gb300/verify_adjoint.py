@@ -9,7 +9,8 @@ from the hand-written adjoint (dugks_autograd.DugksRun, checkpoints every
 `--every` steps, one recomputation per step) and is checked by central
 differences (eps = 1e-6) along `--dirs` seeded random directions
 (splitmix64 seeds 0..dirs-1).  Also reports the cost of the adjoint pass
-(including recomputation) relative to the forward pass.
+(including recomputation) relative to the forward pass, and of one adjoint
+step alone relative to one forward step.
 
   python dugks-gpu_gb300/verify_adjoint.py --precision fp64 --steps 2000 --every 100 --dirs 16
 
@@ -75,7 +76,9 @@ def main():
         fN = da.run(t0, eng, 1, args.steps, every)
         return da.kinetic_energy(eng, fN)
 
-    # forward alone (timing)
+    # forward alone (timing), after one untimed run (first-use costs of the engine and torch)
+    with torch.no_grad():
+        J(u_init, every=args.steps + 1)
     torch.cuda.synchronize()
     t = time.perf_counter()
     with torch.no_grad():
@@ -93,6 +96,23 @@ def main():
     (g,) = torch.autograd.grad(Ju, u)
     torch.cuda.synchronize()
     t_adj = time.perf_counter() - t
+
+    # the adjoint step alone: `every` steps reversed from states recorded beforehand, against
+    # the forward step of the timed forward run
+    with torch.no_grad():
+        f_init = da.from_dump_order(eng, da.feq(rho0, u_init).permute(1, 2, 3, 0))
+        states = torch.empty((args.every, eng.soa_len), dtype=f_init.dtype, device="cuda")
+        stride = states.stride(0) * states.element_size()
+        eng.set_state_device(f_init.data_ptr())
+        eng.run_store(1, args.every, states.data_ptr(), stride)
+        lam_t = torch.ones(eng.soa_len, dtype=f_init.dtype, device="cuda")
+        eng.adjoint_run(1, args.every, states.data_ptr(), stride, lam_t.data_ptr())  # warm-up
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        eng.adjoint_run(1, args.every, states.data_ptr(), stride, lam_t.data_ptr())
+        torch.cuda.synchronize()
+        t_adj_step = (time.perf_counter() - t) / args.every
+        del states
 
     Jfd, extra = J, {}
     if args.precision == "fp32":
@@ -125,6 +145,8 @@ def main():
            "eps": args.eps,
            "forward_s": t_fwd, "forward_with_checkpoints_s": t_fwd_ckpt, "adjoint_s": t_adj,
            "adjoint_over_forward": t_adj / t_fwd,
+           "adjoint_step_ms": 1e3 * t_adj_step, "forward_step_ms": 1e3 * t_fwd / args.steps,
+           "adjoint_step_over_forward_step": t_adj_step / (t_fwd / args.steps),
            "forward_mlups": cells * args.steps / t_fwd / 1e6,
            "adjoint_mlups": cells * args.steps / t_adj / 1e6,
            "checkpoint_states": args.steps // args.every + args.every,

@@ -177,6 +177,16 @@ int dg_set_state_device(dg_t *h, const void *src);
  * f_n; lam_out may equal lam_next.  Asynchronous on the handle's stream. */
 int dg_adjoint_step(dg_t *h, int istep, const void *f_n, const void *lam_next, void *lam_out);
 
+/* Batched forms of the adjoint harness's inner loops (no counterpart in the
+ * reference), asynchronous on the handle's stream:
+ * dg_run_store records in states[s] (s = 0 .. n-1, slots stride_bytes apart,
+ * each one state in the engine's SoA layout) the state from which step
+ * istep0 + s starts, advancing the engine's state by the n - 1 steps in
+ * between; dg_adjoint_run applies the adjoint steps istep0 + n - 1 down to
+ * istep0 to lam in place, step istep0 + s at states[s]. */
+int dg_run_store(dg_t *h, int istep0, int n, void *states, long long stride_bytes);
+int dg_adjoint_run(dg_t *h, int istep0, int n, const void *states, long long stride_bytes, void *lam);
+
 /* Body-force field (no counterpart in the reference; the control variable
  * of the adjoint drag-reduction harness): F(cell) = ambient + phi(cell) e_axis
  * in stage (a), and on a face the mean of phi over its two cells (the one

@@ -73,6 +73,37 @@ def test_adjoint_in_place_equals_out_of_place():
     assert torch.equal(out, lt)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batched_recomputation_and_adjoint_equal_the_step_loops(precision):
+    """dg_run_store / dg_adjoint_run against dg_get_state_device + dg_step and
+    dg_adjoint_step called one at a time: identical arrays."""
+    eng = _engine("stretched", precision)
+    eng.set_stream(torch.cuda.current_stream().cuda_stream)
+    dt = torch.float64 if precision == "fp64" else torch.float32
+    f = da.from_dump_order(eng, torch.from_numpy(seeded_state(eng.nx, eng.ny, eng.nz, seed=23)).cuda().to(dt))
+    n = 5
+    states = torch.zeros((n, eng.soa_len), dtype=dt, device="cuda")
+    stride = states.stride(0) * states.element_size()
+    eng.set_state_device(f.data_ptr())
+    eng.run_store(4, n, states.data_ptr(), stride)
+    ref = torch.zeros_like(states)
+    eng.set_state_device(f.data_ptr())
+    for s in range(n):
+        eng.get_state_device(ref[s].data_ptr())
+        if s + 1 < n:
+            eng.step(4 + s)
+    lam0 = torch.from_numpy(uniform_sym(4, eng.soa_len, 2)).cuda().to(dt)
+    lam_a, lam_b = lam0.clone(), lam0.clone()
+    eng.adjoint_run(4, n, states.data_ptr(), stride, lam_a.data_ptr())
+    for s in reversed(range(n)):
+        eng.adjoint_step(4 + s, ref[s].data_ptr(), lam_b.data_ptr(), lam_b.data_ptr())
+    torch.cuda.synchronize()
+    assert torch.equal(states, ref)
+    assert torch.equal(lam_a, lam_b)
+    with pytest.raises(RuntimeError):
+        eng.adjoint_run(4, n, states.data_ptr(), stride, states[2].data_ptr())  # lam inside the states
+
+
 def _tg_problem(n=16, u0=0.05):
     L = n
     visc = u0 * (L / (2 * np.pi)) / 1600.0
