@@ -86,7 +86,9 @@ def main():
     torch.cuda.synchronize()
     t_fwd = time.perf_counter() - t
 
+    # one untimed gradient (first use of the adjoint kernels and buffers), then the timed one
     u = u_init.clone().requires_grad_(True)
+    torch.autograd.grad(J(u), u)
     torch.cuda.synchronize()
     t = time.perf_counter()
     Ju = J(u)
@@ -140,7 +142,7 @@ def main():
         rels.append(abs(ad - fd) / abs(fd))
     cells = n ** 3
     out = {"workload": f"Taylor-Green vortex {n}^3 periodic, u0=0.05, Re=1600, {args.precision}",
-           "steps": args.steps, "checkpoint_every": args.every, "J": float(Ju),
+           "steps": args.steps, "checkpoint_every": args.every, "J": float(Ju.detach()),
            "fd_rel_err_max": max(rels), "fd_rel_err_median": float(np.median(rels)), "dirs": args.dirs,
            "eps": args.eps,
            "forward_s": t_fwd, "forward_with_checkpoints_s": t_fwd_ckpt, "adjoint_s": t_adj,
