@@ -972,8 +972,9 @@ template <class T, class S, int W, int RECON, int MINB, bool FF>
 __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict__ fb, const S *f_in, S *f_out,
                                                        const StepParams<T, S> P, int kchunk)
 {
+    static_assert(4 * (W - 1) <= 32, "the halo warp evaluates 4 planes x (W-1) rows of -x faces at once");
     __shared__ T ysh[2][W][10][32];  // +y face fluxes of every warp row (double buffer)
-    __shared__ T xsh[2][W][10];      // -x face fluxes of the first column, one per row
+    __shared__ T xsh[2][4][W][10];   // -x face fluxes of the first column: [batch parity][plane of batch][row]
     const int lane = threadIdx.x, wr = threadIdx.y;
     const int nx = P.nx, ny = P.ny, nz = P.nz;
     const int i0 = blockIdx.x * 32 + 1;           // first column of the tile (1-based)
@@ -988,15 +989,19 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict_
     const bool cell = wr >= 1 && gi <= nx && gj <= ny;
     const int ci = min(gi, nx);                     // clamped column for unused lanes
     const int cj = wr >= 1 ? min(gj, ny) : 1;
-    // warp 0 tasks: y face J = j0-1 at column gi; -x face of row j0+lane (lanes < W-1)
-    const int hj = j0 + lane;                       // halo x-face row
-    const bool hx = wr == 0 && lane < W - 1 && hj <= ny;
+    // warp 0 tasks: y face J = j0-1 at column gi every plane; every fourth plane the -x faces
+    // of the first column for the next four planes, lane = q (W-1) + r -> plane +q, row j0+r
+    // (28 of 32 lanes busy, instead of W-1 lanes every plane)
+    const int hq = lane / (W - 1), hr = lane - hq * (W - 1);
+    const int hj = j0 + hr;                         // halo x-face row
+    const bool hx = wr == 0 && hq < 4 && hj <= ny;
 
     T fzd[10], fzu[10], fx[10], fy[10];
     int buf = 0;
     if (kb >= ke) return;
     if (wr >= 1) face_fluxes<T, S, 2, RECON, FF>(P, R, ci, cj, kb - 1, fzd);  // z face kb-1/2
     for (int k = kb; k < ke; ++k) {
+        const int bq = (k - kb) & 3, bp = ((k - kb) >> 2) & 1;  // plane within its batch of four, batch parity
         if (wr >= 1) {
             face_fluxes<T, S, 0, RECON, FF>(P, R, ci, cj, k, fx);   // +x face I = gi
             face_fluxes<T, S, 1, RECON, FF>(P, R, ci, cj, k, fy);   // +y face J = gj
@@ -1007,11 +1012,12 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict_
             face_fluxes<T, S, 1, RECON, FF>(P, R, ci, j0 - 1, k, fy);  // y face J = j0-1 (may be 0: periodic image)
 #pragma unroll
             for (int s = 0; s < 10; ++s) ysh[buf][0][s][lane] = fy[s];
-            if (hx) {
+            // the batch's slots were last read before the barrier of the plane 4 back
+            if (bq == 0 && hx && k + hq < ke) {
                 T hxf[10];
-                face_fluxes<T, S, 0, RECON, FF>(P, R, i0 - 1, hj, k, hxf);  // x face I = i0-1 of row hj
+                face_fluxes<T, S, 0, RECON, FF>(P, R, i0 - 1, hj, k + hq, hxf);  // x face I = i0-1, row hj
 #pragma unroll
-                for (int s = 0; s < 10; ++s) xsh[buf][lane + 1][s] = hxf[s];
+                for (int s = 0; s < 10; ++s) xsh[bp][hq][hr + 1][s] = hxf[s];
             }
         }
         __syncthreads();
@@ -1020,7 +1026,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict_
 #pragma unroll
             for (int s = 0; s < 10; ++s) {
                 const T up = __shfl_up_sync(0xffffffffu, fx[s], 1);
-                fxl[s] = lane == 0 ? xsh[buf][wr][s] : up;
+                fxl[s] = lane == 0 ? xsh[bp][bq][wr][s] : up;
             }
             if (cell) {
                 const long long c = ((long long)(k - 1) * ny + (gj - 1)) * P.pitch + (gi - 1);
