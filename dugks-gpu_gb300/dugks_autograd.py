@@ -110,6 +110,33 @@ def run(f0, eng, istep0, nsteps, every=100):
     return DugksRun.apply(f0, eng, istep0, nsteps, every)
 
 
+class _StatePool:
+    """Slots for the checkpointed states of one schedule, allocated at once:
+    hundreds of separate allocations of a few hundred MB each can cost
+    seconds on a fresh device."""
+
+    def __init__(self, eng, nslots, device):
+        self.buf = torch.empty((nslots, eng.soa_len), dtype=state_dtype(eng), device=device)
+        self.free = list(range(nslots - 1, -1, -1))
+        self.slot = {}
+
+    def store(self, key):
+        """The slot that holds state `key` from now on (its old slot if it has one)."""
+        if key not in self.slot:
+            if not self.free:
+                raise RuntimeError("checkpoint pool exhausted")
+            self.slot[key] = self.free.pop()
+        return self.buf[self.slot[key]]
+
+    def __getitem__(self, key):
+        return self.buf[self.slot[key]]
+
+    def release(self, key):
+        i = self.slot.pop(key, None)
+        if i is not None:
+            self.free.append(i)
+
+
 class DugksObjectiveRun(torch.autograd.Function):
     """(f0, phi) -> (f_n, J), J = (1/n) sum_{k=1..n} objective(f_k, phi).
 
@@ -130,7 +157,8 @@ class DugksObjectiveRun(torch.autograd.Function):
         eng.set_force_field(axis, phi.detach().double().cpu().numpy())
         acts = revolve.actions(nsteps, snaps)
         end, last = revolve.spine(acts)
-        stored = {0: f0.detach().clone()}
+        stored = _StatePool(eng, snaps + 1, f0.device)  # f0 and at most `snaps` more
+        stored.store(0).copy_(f0.detach())
         eng.set_state_device(f0.data_ptr())
         J = torch.zeros((), dtype=torch.float64, device=f0.device)
         phi_d = phi.detach()
@@ -150,9 +178,7 @@ class DugksObjectiveRun(torch.autograd.Function):
                 advance(a[1], a[2])
                 k = a[2]
             else:
-                st = empty_state(eng, f0.device)
-                eng.get_state_device(st.data_ptr())
-                stored[a[1]] = st
+                eng.get_state_device(stored.store(a[1]).data_ptr())
         advance(k, nsteps)
         out = empty_state(eng, f0.device)
         eng.get_state_device(out.data_ptr())
@@ -205,13 +231,11 @@ class DugksObjectiveRun(torch.autograd.Function):
             if kind == "advance":
                 eng.run(istep0 + a[1], a[2] - a[1])
             elif kind == "store":
-                st = empty_state(eng, lam.device)
-                eng.get_state_device(st.data_ptr())
-                stored[a[1]] = st
+                eng.get_state_device(stored.store(a[1]).data_ptr())
             elif kind == "restore":
                 eng.set_state_device(stored[a[1]].data_ptr())
             elif kind == "release":
-                stored.pop(a[1], None)
+                stored.release(a[1])
             else:  # adjoint of step k at the current state k (the engine's own buffer)
                 k = a[1]
                 eng.adjoint_step(istep0 + k, cur.data_ptr(), lam.data_ptr(), lam.data_ptr())

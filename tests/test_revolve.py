@@ -49,3 +49,23 @@ def test_channel_adjoint_budget():
     total, peak = revolve.simulate(4000, 100)
     assert peak == 100
     assert (total - spine_steps) / 4000 < 1.05
+
+
+def test_checkpoint_pool_holds_every_schedule():
+    """The harness's state pool (snaps + 1 slots) runs every schedule without
+    running out, and a restored slot holds what was stored there."""
+    torch = pytest.importorskip("torch")
+    import types
+    import dugks_autograd as da
+    eng = types.SimpleNamespace(soa_len=3, info=types.SimpleNamespace(precision=next(iter(da._TORCH_DTYPE))))
+    for n, free in [(10, 1), (33, 2), (100, 5), (257, 20)]:
+        pool = da._StatePool(eng, free + 1, "cpu")
+        pool.store(0).fill_(0)
+        for a in revolve.actions(n, free):
+            if a[0] == "store":
+                pool.store(a[1]).fill_(a[1])
+            elif a[0] == "restore":
+                assert float(pool[a[1]][0]) == a[1]
+            elif a[0] == "release":
+                pool.release(a[1])
+        assert len(pool.free) + len(pool.slot) == free + 1
