@@ -214,6 +214,52 @@ def cpu_baseline(args, budget_s=12.0):
                       f"oracle/dugks_oracle.c with OpenMP"}
 
 
+def other_configs(k=200, w=3, cpu_budget_s=3.0):
+    """MLUPS of the other single-GPU workloads (they fit in L2, so MLUPS only):
+    the laminar channel (32 x 64 x 32, walls at the wall-normal faces; in the
+    reference orientation 64 wall-normal x 32 x 32) and the Taylor-Green vortex
+    (64^3 periodic, u0 = 0.05, Re = 1600), FP64 and FP32 on the GPU and the
+    oracle (FP64, OpenMP) on the host cores for a bounded number of steps."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import math
+    import pydugks
+    import pyoracle
+    import torch
+    L = 64 / (2 * math.pi)
+    cases = {
+        "laminar channel 32x64x32": dict(case="channel", nx=64, ny=32, nz=32, xwidth=64, ywidth=32, zwidth=32,
+                                         periods_x=0, CFL=0.5, visc=0.032, ambient_fz=6.25e-6),
+        "Taylor-Green 64^3": dict(case="tg_eq", nx=64, ny=64, nz=64, xwidth=64, ywidth=64, zwidth=64, periods_x=1,
+                                  CFL=0.5, visc=f"{0.05 * L / 1600:.9g}", ambient_fz=0.0),
+    }
+    out = {}
+    for name, kw in cases.items():
+        res = {}
+        for prec in ("fp64", "fp32"):
+            with pydugks.Engine(pydugks.make_config(precision=prec, **kw)) as eng:
+                eng.set_stream(torch.cuda.current_stream().cuda_stream)
+                eng.run(1, w)
+                eng.sync()
+                ms = time_steps(eng, w + 1, k)[0]
+                res[prec + "_mlups"] = eng.nx * eng.ny * eng.nz * k / (ms / 1e3) / 1e6
+        with pydugks.Engine(pydugks.make_config(precision="fp64", **kw)) as eng:
+            f0 = eng.get_state()
+            xc, dxx = eng.mesh()
+            orc = pyoracle.Oracle.from_engine_info(eng.info, xc=xc, dxx=dxx)
+            n = eng.nx * eng.ny * eng.nz
+        g = pyoracle.to_ghosted(f0)
+        threads = pyoracle.max_threads()
+        t = time.perf_counter()
+        orc.run(g, 1, 1, threads)
+        steps = max(1, min(400, int(cpu_budget_s / max(time.perf_counter() - t, 1e-4))))
+        t = time.perf_counter()
+        orc.run(g, 2, steps, threads)
+        res["cpu_port_mlups"] = n * steps / (time.perf_counter() - t) / 1e6
+        res["cpu_port_sample"] = f"{steps} steps, {threads} threads"
+        out[name] = res
+    return out
+
+
 def reference_gpu(args, k=10):
     """The reference's own CUDA-C kernels (oracle/_ref cubins, FP64 and its
     PREC4 FP32 build) on the uniform-mesh variant of the same grid (the
@@ -375,6 +421,10 @@ def main():
             extras["cpu_baseline"] = cpu_baseline(args)
         except Exception as e:
             extras["cpu_baseline"] = {"error": str(e)}
+        try:
+            extras["other_configs"] = other_configs()
+        except Exception as e:
+            extras["other_configs"] = {"error": str(e)}
 
     if rank == 0:
         line = {"metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": K, "warmup": W,
