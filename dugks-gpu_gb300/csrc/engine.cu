@@ -12,6 +12,7 @@
 //   dump / read_dump         src/output.cu:22-89
 //   output_2d / save_tecplot_serial / statistics_serial  src/output.cu:118-334
 //   stretched mesh           src/fortran/channel/src/dugks.cuf:107-138, run/mesh.py:21-25
+//   spectral statistics      src/fortran/dhit/src/stat.f90:5-205, main.cuf:83-119 -> dg_spectral_stats()
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -27,9 +28,13 @@
 #include <vector>
 #include <algorithm>
 
+#include <cufft.h>
+#include <dlfcn.h>
+
 #include "../../include/dugks_gb300.h"
 #include "config.h"
 #include "launch.cuh"
+#include "spectral_kernels.cuh"
 
 using namespace dg;
 
@@ -140,6 +145,14 @@ struct dg_ctx {
     CUtensorMap tmap;             // f-bar-plus tensor map of the TMA flux kernel (64-byte aligned type)
     CUtensorMap tmap_adj;         // the same array with the adjoint face kernel's box
     bool have_tmap = false;
+    // spectral statistics (dg_spectral_stats): U, V, W (complex), ET, ETS, partial sums; the
+    // modes grouped by shell (spec_order, spec_off); the cuFFT plan
+    void *spec = nullptr;
+    int *spec_order = nullptr;
+    int *spec_off = nullptr;
+    int spec_nbins = 0;
+    int spec_plan = 0;
+    bool spec_have_plan = false;
     // CUDA graph of kGraphSteps steps, replayed by dg_run when the step's launch
     // parameters do not change from step to step (captured on a private stream)
     cudaStream_t cap_stream = nullptr;
@@ -161,7 +174,12 @@ struct dg_ctx {
         if (dev_err) cudaFree(dev_err);
         if (step_graph) cudaGraphExecDestroy(step_graph);
         if (cap_stream) cudaStreamDestroy(cap_stream);
+        if (spec) cudaFree(spec);
+        if (spec_order) cudaFree(spec_order);
+        if (spec_off) cudaFree(spec_off);
+        release_spec_plan();
     }
+    void release_spec_plan();
     void drop_graph()
     {
         if (step_graph) cudaGraphExecDestroy(step_graph);
@@ -820,6 +838,181 @@ int adjoint_form(dg_ctx *h, int istep, const void *f_n, const void *lam_next, vo
                                  : fn<float, __nv_bfloat16>((h), ##__VA_ARGS__))
 
 // ---------------------------------------------------------------------------
+// spectral statistics of a periodic box (src/fortran/dhit/src/stat.f90:5-205)
+// ---------------------------------------------------------------------------
+// cuFFT is loaded on first use, so that the library itself does not depend on it.
+struct CufftLib {
+    decltype(&cufftPlan3d) plan3d = nullptr;
+    decltype(&cufftExecZ2Z) z2z = nullptr;
+    decltype(&cufftSetStream) set_stream = nullptr;
+    decltype(&cufftDestroy) destroy = nullptr;
+    std::string err;
+};
+
+const CufftLib &cufft_lib()
+{
+    static const CufftLib lib = [] {
+        CufftLib l;
+        void *so = nullptr;
+        for (const char *name : {"libcufft.so.12", "libcufft.so", "/usr/local/cuda/lib64/libcufft.so.12"})
+            if (!so) so = dlopen(name, RTLD_NOW | RTLD_LOCAL);
+        if (!so) {
+            const char *e = dlerror();
+            l.err = std::string("cannot load cuFFT: ") + (e ? e : "unknown error");
+            return l;
+        }
+        l.plan3d = reinterpret_cast<decltype(l.plan3d)>(dlsym(so, "cufftPlan3d"));
+        l.z2z = reinterpret_cast<decltype(l.z2z)>(dlsym(so, "cufftExecZ2Z"));
+        l.set_stream = reinterpret_cast<decltype(l.set_stream)>(dlsym(so, "cufftSetStream"));
+        l.destroy = reinterpret_cast<decltype(l.destroy)>(dlsym(so, "cufftDestroy"));
+        if (!l.plan3d || !l.z2z || !l.set_stream || !l.destroy) l.err = "cuFFT lacks an entry point";
+        return l;
+    }();
+    return lib;
+}
+
+}  // namespace
+
+void dg_ctx::release_spec_plan()
+{
+    if (spec_have_plan && cufft_lib().destroy) cufft_lib().destroy(cufftHandle(spec_plan));
+    spec_have_plan = false;
+}
+
+namespace {
+
+constexpr int kSpecBlocks = 608;  // blocks of the grid-stride reductions (fixed: deterministic sums)
+
+// Values of dg_spectral_stats, in this order.
+enum SpecVal { SV_TE, SV_ETOTAL, SV_EDISS0, SV_EDISS, SV_ETA, SV_VK, SV_TK, SV_UPRM, SV_TMSE, SV_RETMS, SV_XL,
+               SV_KMXETA, SV_SKEW, SV_FLAT, SV_COUNT };
+
+// Buffers, shell lists and plan on first use.
+int spec_setup(dg_ctx *h)
+{
+    const CufftLib &L = cufft_lib();
+    if (!L.err.empty()) return h->fail(DG_ERR_UNSUPPORTED, L.err);
+    const long long n = (long long)h->ncell();
+    if (n >= (1LL << 31)) return h->fail(DG_ERR_UNSUPPORTED, "spectral statistics: more than 2^31 cells");
+    if (!h->spec) {
+        // shells wn = nint(|f|) of the signed integer frequencies (stat.f90:142-151), each shell's
+        // modes in ascending order
+        std::vector<int> bin(static_cast<size_t>(n));
+        int nb = 0;
+        for (int k = 0; k < h->nz; ++k)
+            for (int j = 0; j < h->ny; ++j)
+                for (int i = 0; i < h->nx; ++i) {
+                    const double fx = spec_freq(i, h->nx), fy = spec_freq(j, h->ny), fz = spec_freq(k, h->nz);
+                    const int wn = int(std::lround(std::sqrt(fx * fx + fy * fy + fz * fz)));
+                    bin[(size_t(k) * h->ny + j) * h->nx + i] = wn;
+                    nb = std::max(nb, wn + 1);
+                }
+        std::vector<int> off(static_cast<size_t>(nb) + 1, 0), order(static_cast<size_t>(n));
+        for (long long t = 0; t < n; ++t) ++off[size_t(bin[size_t(t)]) + 1];
+        for (int b = 0; b < nb; ++b) off[size_t(b) + 1] += off[size_t(b)];
+        std::vector<int> fill(off.begin(), off.end() - 1);
+        for (long long t = 0; t < n; ++t) order[size_t(fill[size_t(bin[size_t(t)])]++)] = int(t);
+        const size_t bytes = size_t(n) * (3 * sizeof(double2) + 2 * sizeof(double)) +
+                             size_t(kSpecBlocks) * 3 * sizeof(double) + size_t(nb) * 2 * sizeof(double);
+        CK(cudaMalloc(&h->spec, bytes), "cudaMalloc (spectral statistics)");
+        CK(cudaMalloc(&h->spec_order, size_t(n) * sizeof(int)), "cudaMalloc (spectral shells)");
+        CK(cudaMalloc(&h->spec_off, (size_t(nb) + 1) * sizeof(int)), "cudaMalloc (spectral shells)");
+        CK(cudaMemcpy(h->spec_order, order.data(), size_t(n) * sizeof(int), cudaMemcpyHostToDevice), "shell upload");
+        CK(cudaMemcpy(h->spec_off, off.data(), (size_t(nb) + 1) * sizeof(int), cudaMemcpyHostToDevice),
+           "shell upload");
+        h->spec_nbins = nb;
+    }
+    if (!h->spec_have_plan) {
+        cufftHandle plan;
+        // row-major dims, x fastest: the reference's fftw_plan_dft_3d(nz, ny, nx, ...) (dft.f90:28-34)
+        if (L.plan3d(&plan, h->nz, h->ny, h->nx, CUFFT_Z2Z) != CUFFT_SUCCESS)
+            return h->fail(DG_ERR_CUDA, "cufftPlan3d failed");
+        h->spec_plan = int(plan);
+        h->spec_have_plan = true;
+    }
+    if (L.set_stream(cufftHandle(h->spec_plan), h->stream) != CUFFT_SUCCESS)
+        return h->fail(DG_ERR_CUDA, "cufftSetStream failed");
+    return DG_OK;
+}
+
+template <class T, class S>
+int spectral_form(dg_ctx *h, double *vals, std::vector<double> *shells)
+{
+    int rc = spec_setup(h);
+    if (rc) return rc;
+    const CufftLib &L = cufft_lib();
+    const long long n = (long long)h->ncell();
+    double2 *U = static_cast<double2 *>(h->spec), *V = U + n, *W = V + n;
+    double *ET = reinterpret_cast<double *>(W + n), *ETS = ET + n, *part = ETS + n, *sh = part + kSpecBlocks * 3;
+    StepParams<T, S> P = params_for<T, S>(h, 0);
+    const cufftHandle plan = cufftHandle(h->spec_plan);
+
+    spec_velocity_kernel<T, S><<<kSpecBlocks, 256, 0, h->stream>>>(static_cast<const S *>(h->f), P, U, V, W, part);
+    CK(cudaGetLastError(), "spectral velocity launch");
+    std::vector<double> hp(size_t(kSpecBlocks) * 3);
+    CK(cudaMemcpyAsync(hp.data(), part, kSpecBlocks * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+       "spectral copy");
+    CK(cudaStreamSynchronize(h->stream), "spectral sync");
+    double ke2 = 0;
+    for (int b = 0; b < kSpecBlocks; ++b) ke2 += hp[size_t(b)];
+    for (double2 *X : {U, V, W})
+        if (L.z2z(plan, reinterpret_cast<cufftDoubleComplex *>(X), reinterpret_cast<cufftDoubleComplex *>(X),
+                  CUFFT_FORWARD) != CUFFT_SUCCESS)
+            return h->fail(DG_ERR_CUDA, "cufftExecZ2Z (forward) failed");
+    // the reference's constants: pi = 3.14159 in single precision (stat.f90:28), widths and
+    // viscosity as parsed (float)
+    const double pi = double(3.14159f), L0 = h->xwidth, nu = h->visc;
+    spec_modes_kernel<<<kSpecBlocks, 256, 0, h->stream>>>(U, V, W, ET, ETS, h->nx, h->ny, h->nz, 1.0 / double(n),
+                                                          2 * pi / L0, 2 * nu);
+    CK(cudaGetLastError(), "spectral modes launch");
+    spec_shell_kernel<<<h->spec_nbins, 256, 0, h->stream>>>(ET, ETS, h->spec_order, h->spec_off, sh);
+    CK(cudaGetLastError(), "spectral shells launch");
+    for (double2 *X : {U, V, W})
+        if (L.z2z(plan, reinterpret_cast<cufftDoubleComplex *>(X), reinterpret_cast<cufftDoubleComplex *>(X),
+                  CUFFT_INVERSE) != CUFFT_SUCCESS)
+            return h->fail(DG_ERR_CUDA, "cufftExecZ2Z (inverse) failed");
+    spec_deriv_moments_kernel<<<kSpecBlocks, 256, 0, h->stream>>>(U, V, W, n, part);
+    CK(cudaGetLastError(), "spectral derivative launch");
+    std::vector<double> hs(size_t(h->spec_nbins) * 2);
+    CK(cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+       "spectral copy");
+    CK(cudaMemcpyAsync(hs.data(), sh, hs.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+       "spectral copy");
+    CK(cudaStreamSynchronize(h->stream), "spectral sync");
+    double m2 = 0, m3 = 0, m4 = 0;
+    for (int b = 0; b < kSpecBlocks; ++b) {
+        m2 += hp[size_t(b) * 3];
+        m3 += hp[size_t(b) * 3 + 1];
+        m4 += hp[size_t(b) * 3 + 2];
+    }
+    double etotal = 0, ediss = 0;
+    if (shells) shells->assign(size_t(h->spec_nbins), 0.0);
+    for (int b = 0; b < h->spec_nbins; ++b) {
+        etotal += hs[size_t(b) * 2];
+        ediss += hs[size_t(b) * 2 + 1];
+        if (shells) (*shells)[size_t(b)] = hs[size_t(b) * 2];
+    }
+    // stat.f90:157-168 and 186-190
+    const double nn = double(n), dx = L0 / h->nx, cw = L0, cwh = cw / 2;
+    vals[SV_TE] = 0.5 * ke2 / nn;
+    vals[SV_ETOTAL] = etotal;
+    vals[SV_EDISS0] = ediss;
+    vals[SV_EDISS] = 0.0;
+    vals[SV_ETA] = std::pow(nu * nu * nu / ediss, 0.25);
+    vals[SV_VK] = std::pow(nu * ediss, 0.25);
+    vals[SV_TK] = std::sqrt(nu / ediss);
+    vals[SV_UPRM] = std::sqrt(2.0 / 3.0 * etotal);
+    vals[SV_TMSE] = std::sqrt(15 * nu * vals[SV_UPRM] * vals[SV_UPRM] / ediss);
+    vals[SV_RETMS] = vals[SV_UPRM] * vals[SV_TMSE] / nu;
+    vals[SV_XL] = vals[SV_UPRM] * vals[SV_UPRM] * vals[SV_UPRM] / ediss;
+    vals[SV_KMXETA] = (cwh - 1.5 * dx) * (2 * pi) / cw * vals[SV_ETA];
+    const double bottom = m2 / (3 * nn), top3 = m3 / (3 * nn), top4 = m4 / (3 * nn);
+    vals[SV_SKEW] = top3 / std::pow(bottom, 1.5);
+    vals[SV_FLAT] = top4 / (bottom * bottom);
+    return DG_OK;
+}
+
+// ---------------------------------------------------------------------------
 // allocation and initial condition
 // ---------------------------------------------------------------------------
 template <class T>
@@ -1324,6 +1517,56 @@ int dg_stats(dg_t *h, int step)
     }
     std::fclose(file);
     return rc;
+}
+
+int dg_spectral_stats(dg_t *h, double *vals14, double *spectrum, int nbins)
+{
+    if (!h || nbins < 0 || (nbins > 0 && !spectrum)) return DG_ERR_ARG;
+    if (!h->periodic[0]) return h->fail(DG_ERR_UNSUPPORTED, "spectral statistics need a periodic box (periods_x=1)");
+    double v[SV_COUNT];
+    std::vector<double> sh;
+    const int rc = DISPATCH(h, spectral_form, v, &sh);
+    if (rc) return rc;
+    if (vals14) std::memcpy(vals14, v, sizeof(v));
+    for (int b = 0; b < nbins; ++b) spectrum[b] = b < int(sh.size()) ? sh[size_t(b)] : 0.0;
+    return DG_OK;
+}
+
+int dg_output_spectral(dg_t *h, int step)
+{
+    if (!h) return DG_ERR_ARG;
+    if (!h->periodic[0]) return h->fail(DG_ERR_UNSUPPORTED, "spectral statistics need a periodic box (periods_x=1)");
+    double v[SV_COUNT];
+    std::vector<double> sh;
+    const int rc = DISPATCH(h, spectral_form, v, &sh);
+    if (rc) return rc;
+    const double dt = h->prec == DG_PREC_FP64 ? h->c64.dt : double(h->c32.dt), t = step * dt;
+    auto append = [&](const char *name) -> FILE * { return std::fopen((h->workdir + "/" + name).c_str(), "a"); };
+    FILE *fp = append("KE.dat");  // (I6.6,1X,F12.5,1X,1pe16.9)
+    if (!fp) return h->fail(DG_ERR_IO, "cannot append KE.dat");
+    std::fprintf(fp, "%06d %12.5f %16.9E\n", step, t, v[SV_TE]);
+    std::fclose(fp);
+    fp = append("stat_te.dat");  // (I7,1X,F16.8,1X,1pe15.6)
+    if (!fp) return h->fail(DG_ERR_IO, "cannot append stat_te.dat");
+    std::fprintf(fp, "%7d %16.8f %15.6E\n", step, t, v[SV_TE]);
+    std::fclose(fp);
+    fp = append("stat_te_spectral.dat");  // (I7,1X,F16.8,1X,3(1pe15.6,1X),8(1pe15.6,1X))
+    if (!fp) return h->fail(DG_ERR_IO, "cannot append stat_te_spectral.dat");
+    std::fprintf(fp, "%7d %16.8f ", step, t);
+    for (int q = SV_ETOTAL; q <= SV_KMXETA; ++q) std::fprintf(fp, "%15.6E ", v[q]);
+    std::fprintf(fp, "\n");
+    std::fclose(fp);
+    char name[32];
+    std::snprintf(name, sizeof(name), "spe%9.9d.dat", step);  // (I4,1X,1pe15.6), shells 0..nx
+    fp = std::fopen((h->workdir + "/" + name).c_str(), "w");
+    if (!fp) return h->fail(DG_ERR_IO, std::string("cannot write ") + name);
+    for (int b = 0; b <= h->nx; ++b) std::fprintf(fp, "%4d %15.6E\n", b, b < int(sh.size()) ? sh[size_t(b)] : 0.0);
+    std::fclose(fp);
+    fp = append("skew-flat.dat");  // (I7,1X,1pe15.6,1X,1pe15.6,1X,1pe15.6)
+    if (!fp) return h->fail(DG_ERR_IO, "cannot append skew-flat.dat");
+    std::fprintf(fp, "%7d %15.6E %15.6E %15.6E\n", step, t, v[SV_SKEW], v[SV_FLAT]);
+    std::fclose(fp);
+    return DG_OK;
 }
 
 int dg_output_2d(dg_t *h, int step)

@@ -104,6 +104,8 @@ def lib():
                                                     ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                                     ctypes.c_void_p, ctypes.c_void_p]),
         "dg_noalloc_last_error": (ctypes.c_char_p, []),
+        "dg_spectral_stats": (ctypes.c_int, [H, _D, _D, ctypes.c_int]),
+        "dg_output_spectral": (ctypes.c_int, [H, ctypes.c_int]),
         "dg_get_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
         "dg_set_state_device": (ctypes.c_int, [H, ctypes.c_void_p]),
         "dg_adjoint_step": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
@@ -327,6 +329,20 @@ class Engine:
     def adjoint_step(self, istep, f_ptr, lam_next_ptr, lam_out_ptr):
         self._check(lib().dg_adjoint_step(self._h, istep, ctypes.c_void_p(f_ptr), ctypes.c_void_p(lam_next_ptr),
                                           ctypes.c_void_p(lam_out_ptr)))
+
+    SPECTRAL_KEYS = ("te", "etotal", "ediss", "ediss_total", "eta", "vk", "tk", "uprm", "tmse", "retms", "xl",
+                     "kmxeta", "skew", "flat")
+
+    def spectral_stats(self, nbins=None):
+        """(dict of the 14 values of dg_spectral_stats, shell spectrum E(k) for k = 0..nbins-1)."""
+        nb = self.nx + 1 if nbins is None else int(nbins)
+        vals = np.zeros(14)
+        spec = np.zeros(max(nb, 1))
+        self._check(lib().dg_spectral_stats(self._h, _ptr(vals), _ptr(spec), nb))
+        return dict(zip(self.SPECTRAL_KEYS, vals.tolist())), spec[:nb]
+
+    def output_spectral(self, step):
+        self._check(lib().dg_output_spectral(self._h, step))
 
     def run_store(self, istep0, n, states_ptr, stride_bytes):
         self._check(lib().dg_run_store(self._h, istep0, n, ctypes.c_void_p(states_ptr), stride_bytes))

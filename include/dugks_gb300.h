@@ -131,6 +131,23 @@ int dg_stats(dg_t *h, int step);
  * src/output.cu:152-218 (output_2d, src/output.cu:118-147). */
 int dg_output_2d(dg_t *h, int step);
 
+/* Spectral statistics of a periodic box: the statistics of the reference's
+ * Fortran decaying-turbulence code (src/fortran/dhit/src/stat.f90:5-205) from
+ * the current state, u = j/rho (src/fortran/dhit/src/main.cuf:86-103), on
+ * the device with cuFFT (loaded on first use), in FP64.  vals14 (may be
+ * NULL): kinetic energy 0.5<|u|^2>, spectral energy, dissipation, 0 (the
+ * reference's ediss_total), Kolmogorov length, velocity and time, u', Taylor
+ * microscale, Taylor Reynolds number, large-eddy length, kmax*eta, skewness
+ * and flatness of the longitudinal derivatives.  spectrum (may be NULL):
+ * shell energies E(k), k = 0 .. nbins-1 (zero past the last shell).  Needs
+ * periods_x=1 (DG_ERR_UNSUPPORTED otherwise). */
+int dg_spectral_stats(dg_t *h, double *vals14, double *spectrum, int nbins);
+
+/* dg_spectral_stats written as the reference writes it for step `step`:
+ * KE.dat (main.cuf:114-116), stat_te.dat, stat_te_spectral.dat, skew-flat.dat
+ * (appended) and spe%09d.dat (stat.f90:60-62, 170-182, 192-194). */
+int dg_output_spectral(dg_t *h, int step);
+
 /* Time-averaged statistics (an extension; the reference writes instantaneous
  * profiles only): dg_stats_accumulate adds the current per-x plane sums of
  * u, v, w and their products into FP64 device accumulators;
