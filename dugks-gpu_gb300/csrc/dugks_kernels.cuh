@@ -129,22 +129,28 @@ __device__ __forceinline__ void feq_pair(T eu, T base, T wr, T &fp, T &fm)
     fm = fma(-wr, eu, wt);
 }
 
-// Zeroth and first moments of 19 values.  Summed as balanced trees (the
-// reference sums sequentially over ip, src/dugks.cu:687-693): same values to
-// rounding, with a dependency chain of 5 additions instead of 18 -- the
-// reduced-rate FP64 pipe of GB300 is latency-bound on long chains.
+// Zeroth and first moments of 19 values, from the sums and differences of the
+// nine opposite pairs (18 operations): rho from the nine sums, each momentum
+// component from its five differences -- 39 operations instead of 45 for the
+// direct sums (the reference sums sequentially over ip, src/dugks.cu:687-693:
+// same values to rounding), in short dependency chains for the reduced-rate
+// FP64 pipe of GB300.
 template <class T>
 __device__ __forceinline__ void moments(const T v[NPOP], T &r, T &jx, T &jy, T &jz)
 {
-    const T a = (v[0] + v[1]) + (v[2] + v[3]);
-    const T b = (v[4] + v[5]) + (v[6] + v[7]);
-    const T c = (v[8] + v[9]) + (v[10] + v[11]);
-    const T d = (v[12] + v[13]) + (v[14] + v[15]);
-    const T e = (v[16] + v[17]) + v[18];
-    r = ((a + b) + (c + d)) + e;
-    jx = ((v[1] - v[2]) + (v[7] - v[8])) + ((v[9] - v[10]) + (v[11] - v[12])) + (v[13] - v[14]);
-    jy = ((v[3] - v[4]) + (v[7] + v[8])) + ((v[15] - v[16]) + (v[17] - v[18])) - (v[9] + v[10]);
-    jz = ((v[5] - v[6]) + (v[11] + v[12])) + ((v[15] + v[16]) - (v[17] + v[18])) - (v[13] + v[14]);
+    const T s1 = v[1] + v[2], d1 = v[1] - v[2];          // (+-1, 0, 0)
+    const T s3 = v[3] + v[4], d3 = v[3] - v[4];          // (0, +-1, 0)
+    const T s5 = v[5] + v[6], d5 = v[5] - v[6];          // (0, 0, +-1)
+    const T s7 = v[7] + v[10], d7 = v[7] - v[10];        // 7 = (1, 1, 0)
+    const T s8 = v[8] + v[9], d8 = v[8] - v[9];          // 8 = (-1, 1, 0)
+    const T s11 = v[11] + v[14], d11 = v[11] - v[14];    // 11 = (1, 0, 1)
+    const T s12 = v[12] + v[13], d12 = v[12] - v[13];    // 12 = (-1, 0, 1)
+    const T s15 = v[15] + v[18], d15 = v[15] - v[18];    // 15 = (0, 1, 1)
+    const T s16 = v[16] + v[17], d16 = v[16] - v[17];    // 16 = (0, -1, 1)
+    r = ((v[0] + s1) + (s3 + s5)) + ((s7 + s8) + (s11 + s12)) + (s15 + s16);
+    jx = ((d1 + d7) - d8) + (d11 - d12);
+    jy = ((d3 + d7) + d8) + (d15 - d16);
+    jz = ((d5 + d11) + d12) + (d15 + d16);
 }
 
 // 1/r: FP64 from a single-precision seed and two Newton steps (error at the
