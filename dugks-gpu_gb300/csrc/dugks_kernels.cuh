@@ -153,17 +153,16 @@ __device__ __forceinline__ void moments(const T v[NPOP], T &r, T &jx, T &jy, T &
     jz = ((d5 + d11) + d12) + (d15 + d16);
 }
 
-// 1/r: FP64 from a single-precision seed and two Newton steps (error at the
-// rounding level), cheaper than the full-precision divide on the FP64 pipe;
-// the correctly rounded FP32 reciprocal (same result as 1.0f / r, without the
-// division's multi-instruction sequence) for FP32.
+// 1/r: FP64 from a single-precision seed x (relative error e ~ 2^-23) and one
+// third-order correction x (1 + e + e^2) (truncation error ~e^3, far below the
+// rounding level): three dependent FMAs, cheaper than the full-precision
+// divide on the FP64 pipe; the correctly rounded FP32 reciprocal (same result
+// as 1.0f / r, without the division's multi-instruction sequence) for FP32.
 __device__ __forceinline__ double recip(double r)
 {
-    double x = double(__frcp_rn(float(r)));
-    double e = fma(-r, x, 1.0);
-    x = fma(x, e, x);
-    e = fma(-r, x, 1.0);
-    return fma(x, e, x);
+    const double x = double(__frcp_rn(float(r)));
+    const double e = fma(-r, x, 1.0);
+    return fma(x, fma(e, e, e), x);
 }
 __device__ __forceinline__ float recip(float r) { return __frcp_rn(r); }
 
