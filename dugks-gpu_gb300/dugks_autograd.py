@@ -113,12 +113,28 @@ def run(f0, eng, istep0, nsteps, every=100):
 class _StatePool:
     """Slots for the checkpointed states of one schedule, allocated at once:
     hundreds of separate allocations of a few hundred MB each can cost
-    seconds on a fresh device."""
+    seconds on a fresh device.  `for_engine` keeps one pool per engine and
+    reuses it while the slot count and layout match (the memory stays
+    allocated while the engine object lives)."""
 
     def __init__(self, eng, nslots, device):
         self.buf = torch.empty((nslots, eng.soa_len), dtype=state_dtype(eng), device=device)
-        self.free = list(range(nslots - 1, -1, -1))
+        self.reset()
+
+    def reset(self):
+        self.free = list(range(self.buf.shape[0] - 1, -1, -1))
         self.slot = {}
+
+    @staticmethod
+    def for_engine(eng, nslots, device):
+        pool = getattr(eng, "_dg_state_pool", None)
+        if (pool is None or pool.buf.shape != (nslots, eng.soa_len) or pool.buf.dtype != state_dtype(eng)
+                or pool.buf.device != torch.device(device)):
+            eng._dg_state_pool = None  # release the old pool before allocating the new one
+            pool = _StatePool(eng, nslots, device)
+            eng._dg_state_pool = pool
+        pool.reset()
+        return pool
 
     def store(self, key):
         """The slot that holds state `key` from now on (its old slot if it has one)."""
@@ -157,7 +173,7 @@ class DugksObjectiveRun(torch.autograd.Function):
         eng.set_force_field(axis, phi.detach().double().cpu().numpy())
         acts = revolve.actions(nsteps, snaps)
         end, last = revolve.spine(acts)
-        stored = _StatePool(eng, snaps + 1, f0.device)  # f0 and at most `snaps` more
+        stored = _StatePool.for_engine(eng, snaps + 1, f0.device)  # f0 and at most `snaps` more
         stored.store(0).copy_(f0.detach())
         eng.set_state_device(f0.data_ptr())
         J = torch.zeros((), dtype=torch.float64, device=f0.device)
