@@ -279,6 +279,47 @@ __device__ __forceinline__ void copy_images(S *fb, long long ps_b, int I, int J,
 // plain path.  xoff shifts the cells by one thread when nx = 1 (mod 32) so
 // that cells nx-1 and nx share a warp.  The result equals the reference's
 // x -> y -> z fill order.
+// Stage (a) with a force along axis A only (FP64 form): f-bar-plus_p =
+// (B + K_p) feq_p + bw1 f_p with K_p in {0, +-Kb}, fused per opposite pair
+// (p, q): feq_{p,q} = w r (t +- eu), t = base + eu^2/2.  A pair with c_A = 0
+// shares K = B w r:  K t + (bw1 f_p) +- K eu  (7 operations for the pair, 9
+// for the equilibria followed by the combines); a pair along A has
+// K_{p,q} = (B +- Kb) w r:  K_p (t + eu) + bw1 f_p  (8 operations).
+template <class T, int A>
+__device__ __forceinline__ void fbar_one_axis(T r, T u, T vv, T w, T B, T Kb, T bw1, const T v[NPOP], T ob[NPOP])
+{
+    const T u3 = T(3) * u, v3 = T(3) * vv, w3 = T(3) * w;
+    const T base = fma(T(-1.5), fma(u, u, fma(vv, vv, w * w)), T(1));
+    const T wr0 = weight<T>(0) * r, wr1 = weight<T>(1) * r, wr2 = weight<T>(7) * r;
+    const T Bp = B + Kb, Bm = B - Kb;
+    const T K1 = B * wr1, K2 = B * wr2, Kp1 = Bp * wr1, Km1 = Bm * wr1, Kp2 = Bp * wr2, Km2 = Bm * wr2;
+    ob[0] = fma(B * wr0, base, bw1 * v[0]);
+    auto pair = [&](int p, int q, T eu, int cls) {
+        const T t = fma(T(0.5) * eu, eu, base);
+        const int ca = cc(A, p);
+        if (ca == 0) {
+            const T K = cls == 1 ? K1 : K2;
+            const T X = K * t;
+            ob[p] = fma(K, eu, fma(bw1, v[p], X));
+            ob[q] = fma(-K, eu, fma(bw1, v[q], X));
+        } else {
+            const T Kp = cls == 1 ? (ca > 0 ? Kp1 : Km1) : (ca > 0 ? Kp2 : Km2);
+            const T Kq = cls == 1 ? (ca > 0 ? Km1 : Kp1) : (ca > 0 ? Km2 : Kp2);
+            ob[p] = fma(Kp, t + eu, bw1 * v[p]);
+            ob[q] = fma(Kq, t - eu, bw1 * v[q]);
+        }
+    };
+    pair(1, 2, u3, 1);
+    pair(3, 4, v3, 1);
+    pair(5, 6, w3, 1);
+    pair(7, 10, u3 + v3, 2);
+    pair(8, 9, v3 - u3, 2);
+    pair(11, 14, u3 + w3, 2);
+    pair(12, 13, w3 - u3, 2);
+    pair(15, 18, v3 + w3, 2);
+    pair(16, 17, w3 - v3, 2);
+}
+
 template <class T, class S, bool GHOST>
 __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *__restrict__ fb, const StepParams<T, S> P,
                                                    int xoff)
@@ -329,32 +370,30 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
         B = fma(-P.bw0x3, fma(Fx, u, fma(Fy, vv, Fz * w)), P.bw2);
     }
 
-    T fe[NPOP];
-    feq_all(r, u, vv, w, fe);
     const unsigned hc = P.codec.cell_hash(cb);
-    auto fbar_p = [&](int p) -> T {
-        T K = P.Kb[p];
-        if (P.perturb || P.ffield) {
-            T cf = T(0);
-            if (cx(p)) cf += cx(p) > 0 ? Fx : -Fx;
-            if (cy(p)) cf += cy(p) > 0 ? Fy : -Fy;
-            if (cz(p)) cf += cz(p) > 0 ? Fz : -Fz;
-            K = P.bw0x3 * cf;
-        }
-        return fma(B + K, fe[p], P.bw1 * v[p]);
-    };
     T ob[NPOP];
     if (one_axis) {
-        const T Bp = B + P.Kba, Bm = B - P.Kba;
-        const int a = P.fax;
+        if (P.fax == 0)
+            fbar_one_axis<T, 0>(r, u, vv, w, B, P.Kba, P.bw1, v, ob);
+        else if (P.fax == 1)
+            fbar_one_axis<T, 1>(r, u, vv, w, B, P.Kba, P.bw1, v, ob);
+        else
+            fbar_one_axis<T, 2>(r, u, vv, w, B, P.Kba, P.bw1, v, ob);
+    } else {
+        T fe[NPOP];
+        feq_all(r, u, vv, w, fe);
 #pragma unroll
         for (int p = 0; p < NPOP; ++p) {
-            const int ca = a == 0 ? cx(p) : (a == 1 ? cy(p) : cz(p));
-            ob[p] = fma(ca > 0 ? Bp : (ca < 0 ? Bm : B), fe[p], P.bw1 * v[p]);
+            T K = P.Kb[p];
+            if (P.perturb || P.ffield) {
+                T cf = T(0);
+                if (cx(p)) cf += cx(p) > 0 ? Fx : -Fx;
+                if (cy(p)) cf += cy(p) > 0 ? Fy : -Fy;
+                if (cz(p)) cf += cz(p) > 0 ? Fz : -Fz;
+                K = P.bw0x3 * cf;
+            }
+            ob[p] = fma(B + K, fe[p], P.bw1 * v[p]);
         }
-    } else {
-#pragma unroll
-        for (int p = 0; p < NPOP; ++p) ob[p] = fbar_p(p);
     }
     if (sizeof(T) == 4) {
         // FP32 arithmetic: the moments of f-bar-plus are set to their exact values
