@@ -24,6 +24,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "d3q19.cuh"
 #include "storage.cuh"
@@ -691,6 +692,152 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
     }
 }
 
+// face_tri for the FP32 form on packed pairs (sm_100+ FMUL2/FFMA2): the 18
+// moving populations of a face form nine pairs (p, q) with the same stencil
+// shape -- the same rows, planes and lerps, weights of the same kind -- whose
+// lerps run two per instruction, each half rounded as the scalar instruction.
+// A lerp is m b + (om a) here (one rounding order of face_tri's om a + m b).
+// Pairs per face orientation: first populations kPairP[AX], second kPairQ[AX];
+// a mixed-class pair has its c_x > 0 population first.
+__host__ __device__ constexpr int pair_p(int ax, int n)
+{
+    return ax == 0 ? (n == 0 ? 1 : n == 1 ? 3 : n == 2 ? 7 : n == 3 ? 9 : n == 4 ? 5 : n == 5 ? 11 : n == 6 ? 13 : n == 7 ? 15 : 17)
+         : ax == 1 ? (n == 0 ? 3 : n == 1 ? 1 : n == 2 ? 7 : n == 3 ? 9 : n == 4 ? 5 : n == 5 ? 15 : n == 6 ? 17 : n == 7 ? 11 : 13)
+                   : (n == 0 ? 5 : n == 1 ? 1 : n == 2 ? 11 : n == 3 ? 13 : n == 4 ? 3 : n == 5 ? 15 : n == 6 ? 17 : n == 7 ? 7 : 9);
+}
+__host__ __device__ constexpr int pair_q(int ax, int n) { return pair_p(ax, n) + 1; }
+
+__device__ __forceinline__ float2 lerp_x2(float2 om, float2 m, float2 a, float2 b)
+{
+    return __ffma2_rn(m, b, __fmul2_rn(om, a));
+}
+
+template <class S, int AX, class RD>
+__device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const RD &R, int i, int j, int k,
+                                            float v[NPOP])
+{
+    using RI = decltype(R.rb(0, 0));
+    const int jm = j - 1, jp = j + 1, jc = j;
+    const int km = k - 1, kp = k + 1, kc = k;
+    const int xs = P.xws;
+    const float2 ty_o = make_float2(P.ty_om, P.ty_om), ty_m = make_float2(P.ty_m, P.ty_m);
+    const float2 tz_o = make_float2(P.tz_om, P.tz_om), tz_m = make_float2(P.tz_m, P.tz_m);
+    if (AX == 0) {
+        const int A = i == 0 ? 1 : i, B = i == 0 ? 0 : i + 1;
+        const float *xw = P.xw + i;
+        const float2 om12 = make_float2(__ldg(xw + 2 * xs), __ldg(xw + 4 * xs));
+        const float2 m12 = make_float2(__ldg(xw + 3 * xs), __ldg(xw + 5 * xs));
+        const float om3 = __ldg(xw + 6 * xs), m3 = __ldg(xw + 7 * xs);
+        const float2 om33 = make_float2(om3, om3), m33 = make_float2(m3, m3);
+        const RI r00 = R.rb(jc, kc);
+        v[0] = R.dec(0, 0.5f * (R.raw(0, r00, A) + R.raw(0, r00, B)));
+#pragma unroll
+        for (int n = 0; n < 9; ++n) {
+            const int p = pair_p(0, n), q = pair_q(0, n);
+            const bool ay = cy(p) != 0, az = cz(p) != 0;
+            const float2 om = xrep(p) == 3 ? om33 : om12, m = xrep(p) == 3 ? m33 : m12;
+            const int jtp = cy(p) > 0 ? jm : (cy(p) < 0 ? jp : jc), jtq = cy(q) > 0 ? jm : (cy(q) < 0 ? jp : jc);
+            const int ktp = cz(p) > 0 ? km : (cz(p) < 0 ? kp : kc), ktq = cz(q) > 0 ? km : (cz(q) < 0 ? kp : kc);
+            const float2 x00 = lerp_x2(om, m, make_float2(R.raw(p, r00, A), R.raw(q, r00, A)),
+                                       make_float2(R.raw(p, r00, B), R.raw(q, r00, B)));
+            float2 y00 = x00;
+            if (ay) {
+                const RI sp = R.rb(jtp, kc), sq = R.rb(jtq, kc);
+                const float2 x01 = lerp_x2(om, m, make_float2(R.raw(p, sp, A), R.raw(q, sq, A)),
+                                           make_float2(R.raw(p, sp, B), R.raw(q, sq, B)));
+                y00 = lerp_x2(ty_o, ty_m, x00, x01);
+            }
+            float2 res = y00;
+            if (az) {
+                const RI tp = R.rb(jc, ktp), tq = R.rb(jc, ktq);
+                const float2 x10 = lerp_x2(om, m, make_float2(R.raw(p, tp, A), R.raw(q, tq, A)),
+                                           make_float2(R.raw(p, tp, B), R.raw(q, tq, B)));
+                float2 y11 = x10;
+                if (ay) {
+                    const RI up = R.rb(jtp, ktp), uq = R.rb(jtq, ktq);
+                    const float2 x11 = lerp_x2(om, m, make_float2(R.raw(p, up, A), R.raw(q, uq, A)),
+                                               make_float2(R.raw(p, up, B), R.raw(q, uq, B)));
+                    y11 = lerp_x2(ty_o, ty_m, x10, x11);
+                }
+                res = lerp_x2(tz_o, tz_m, y00, y11);
+            }
+            v[p] = R.dec(p, res.x);
+            v[q] = R.dec(q, res.y);
+        }
+    } else if (AX == 1) {
+        // rows j (A) and j+1 (B); transverse x to column i - cx, z to plane k - cz
+        const RI rA = R.rb(jc, kc), rB = R.rb(jp, kc);
+        v[0] = R.dec(0, 0.5f * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+        const float *tw = P.txw + i;
+        const float2 tx_o = make_float2(__ldg(tw + 2 * xs), __ldg(tw + 4 * xs));
+        const float2 tx_m = make_float2(__ldg(tw + 3 * xs), __ldg(tw + 5 * xs));
+#pragma unroll
+        for (int n = 0; n < 9; ++n) {
+            const int p = pair_p(1, n), q = pair_q(1, n);
+            const bool ax = cx(p) != 0, az = cz(p) != 0;
+            const int iop = i - cx(p), ioq = i - cx(q);
+            const int ktp = cz(p) > 0 ? km : (cz(p) < 0 ? kp : kc), ktq = cz(q) > 0 ? km : (cz(q) < 0 ? kp : kc);
+            const float2 yo = make_float2(P.yn_om[p], P.yn_om[q]), ym = make_float2(P.yn_m[p], P.yn_m[q]);
+            float2 x00 = make_float2(R.raw(p, rA, i), R.raw(q, rA, i));
+            float2 x01 = make_float2(R.raw(p, rB, i), R.raw(q, rB, i));
+            if (ax) {
+                x00 = lerp_x2(tx_o, tx_m, x00, make_float2(R.raw(p, rA, iop), R.raw(q, rA, ioq)));
+                x01 = lerp_x2(tx_o, tx_m, x01, make_float2(R.raw(p, rB, iop), R.raw(q, rB, ioq)));
+            }
+            const float2 y00 = lerp_x2(yo, ym, x00, x01);
+            float2 res = y00;
+            if (az) {
+                const RI sAp = R.rb(jc, ktp), sBp = R.rb(jp, ktp), sAq = R.rb(jc, ktq), sBq = R.rb(jp, ktq);
+                float2 x10 = make_float2(R.raw(p, sAp, i), R.raw(q, sAq, i));
+                float2 x11 = make_float2(R.raw(p, sBp, i), R.raw(q, sBq, i));
+                if (ax) {
+                    x10 = lerp_x2(tx_o, tx_m, x10, make_float2(R.raw(p, sAp, iop), R.raw(q, sAq, ioq)));
+                    x11 = lerp_x2(tx_o, tx_m, x11, make_float2(R.raw(p, sBp, iop), R.raw(q, sBq, ioq)));
+                }
+                res = lerp_x2(tz_o, tz_m, y00, lerp_x2(yo, ym, x10, x11));
+            }
+            v[p] = R.dec(p, res.x);
+            v[q] = R.dec(q, res.y);
+        }
+    } else {
+        // planes k (A) and k+1 (B); transverse x to column i - cx, y to row j - cy
+        const RI rA = R.rb(jc, kc), rB = R.rb(jc, kp);
+        v[0] = R.dec(0, 0.5f * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+        const float *tw = P.txw + i;
+        const float2 tx_o = make_float2(__ldg(tw + 2 * xs), __ldg(tw + 4 * xs));
+        const float2 tx_m = make_float2(__ldg(tw + 3 * xs), __ldg(tw + 5 * xs));
+#pragma unroll
+        for (int n = 0; n < 9; ++n) {
+            const int p = pair_p(2, n), q = pair_q(2, n);
+            const bool ax = cx(p) != 0, ay = cy(p) != 0;
+            const int iop = i - cx(p), ioq = i - cx(q);
+            const int jtp = cy(p) > 0 ? jm : (cy(p) < 0 ? jp : jc), jtq = cy(q) > 0 ? jm : (cy(q) < 0 ? jp : jc);
+            const float2 zo = make_float2(P.zn_om[p], P.zn_om[q]), zm = make_float2(P.zn_m[p], P.zn_m[q]);
+            float2 x00 = make_float2(R.raw(p, rA, i), R.raw(q, rA, i));
+            float2 x10 = make_float2(R.raw(p, rB, i), R.raw(q, rB, i));
+            if (ax) {
+                x00 = lerp_x2(tx_o, tx_m, x00, make_float2(R.raw(p, rA, iop), R.raw(q, rA, ioq)));
+                x10 = lerp_x2(tx_o, tx_m, x10, make_float2(R.raw(p, rB, iop), R.raw(q, rB, ioq)));
+            }
+            float2 y00 = x00, y11 = x10;
+            if (ay) {
+                const RI sAp = R.rb(jtp, kc), sBp = R.rb(jtp, kp), sAq = R.rb(jtq, kc), sBq = R.rb(jtq, kp);
+                float2 x01 = make_float2(R.raw(p, sAp, i), R.raw(q, sAq, i));
+                float2 x11 = make_float2(R.raw(p, sBp, i), R.raw(q, sBq, i));
+                if (ax) {
+                    x01 = lerp_x2(tx_o, tx_m, x01, make_float2(R.raw(p, sAp, iop), R.raw(q, sAq, ioq)));
+                    x11 = lerp_x2(tx_o, tx_m, x11, make_float2(R.raw(p, sBp, iop), R.raw(q, sBq, ioq)));
+                }
+                y00 = lerp_x2(ty_o, ty_m, x00, x01);
+                y11 = lerp_x2(ty_o, ty_m, x10, x11);
+            }
+            const float2 res = lerp_x2(zo, zm, y00, y11);
+            v[p] = R.dec(p, res.x);
+            v[q] = R.dec(q, res.y);
+        }
+    }
+}
+
 // Corner-weight form of face_tri for the FP64 step, whose throughput is set by
 // the FP64 instruction count: each face value is sum_q w_q f_q over its 2, 4
 // or 8 stencil points (one multiply and FMAs) instead of the nested lerps
@@ -1002,9 +1149,11 @@ template <class T, class S, int AX, int RECON, bool FF, class RD>
 __device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const RD &R, int i, int j, int k, T out[10])
 {
     T v[NPOP];
-    if (RECON == 0 && Fp64Form<T>::value)
+    if constexpr (RECON == 0 && Fp64Form<T>::value)
         face_tri_cw<T, S, AX>(P, R, i, j, k, v);
-    else if (RECON == 0)
+    else if constexpr (RECON == 0 && std::is_same<S, float>::value)
+        face_tri_x2<S, AX>(P, R, i, j, k, v);  // FP32 form (the 16-bit forms measured slower packed)
+    else if constexpr (RECON == 0)
         face_tri<T, S, AX>(P, R, i, j, k, v);
     else
         face_grad<T, S, AX>(P, R, i, j, k, v);
