@@ -707,6 +707,30 @@ __host__ __device__ constexpr int pair_p(int ax, int n)
 }
 __host__ __device__ constexpr int pair_q(int ax, int n) { return pair_p(ax, n) + 1; }
 
+// The pairing rule, checked at compile time: per orientation every moving
+// population once; the two of a pair with the same transverse lerps (c != 0
+// on the same transverse axes) and x weights of one kind: both c_x = 0, or
+// c_x > 0 first and c_x < 0 second (the packed x-weight pairs).
+__host__ __device__ constexpr bool face_pairs_ok()
+{
+    for (int ax = 0; ax < 3; ++ax) {
+        int seen = 0;
+        for (int n = 0; n < 9; ++n) {
+            const int p = pair_p(ax, n), q = pair_q(ax, n);
+            if (p < 1 || q > 18) return false;
+            seen |= (1 << p) | (1 << q);
+            for (int t = 0; t < 3; ++t)
+                if (t != ax && (cc(t, p) != 0) != (cc(t, q) != 0)) return false;
+            const bool x_lerp = ax != 0 && cx(p) != 0;   // transverse x lerp (y, z faces)
+            const bool x_face = ax == 0;                   // x-face normal weights by class
+            if ((x_lerp || x_face) && !(cx(p) == 0 && cx(q) == 0) && !(cx(p) > 0 && cx(q) < 0)) return false;
+        }
+        if (seen != ((1 << 19) - 2)) return false;
+    }
+    return true;
+}
+static_assert(face_pairs_ok(), "face population pairs of face_tri_x2 must share their stencil shape");
+
 __device__ __forceinline__ float2 lerp_x2(float2 om, float2 m, float2 a, float2 b)
 {
     return __ffma2_rn(m, b, __fmul2_rn(om, a));
