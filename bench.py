@@ -52,10 +52,30 @@ def dist_env():
 
 
 def workload(args, precision):
-    import pydugks
+    import workloads
     nx, ny, nz = (int(v) for v in args.grid.split(","))
-    cfg, meta = pydugks.channel_config(nx=nx, ny=ny, nz=nz, precision=precision)
+    cfg, meta = workloads.channel_config(nx=nx, ny=ny, nz=nz, precision=precision)
     return cfg, meta, (nx, ny, nz)
+
+
+def bench_config(args, meta, grid, world):
+    """The `config` object of the JSON line, the same for both arms."""
+    n = grid[0] * grid[1] * grid[2]
+    return {"workload": describe(grid, args.precision), "grid_nx_ny_nz": list(grid), "mesh": "tanh",
+            "re_tau": 180, "nu": meta["nu"], "alpha": meta["alpha"], "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (f and f-bar-plus resident, %d MB each)"
+                  % (n * 19 * {"fp64": 8, "fp32": 4}.get(args.precision, 2) // 2**20),
+            "structure": "two-pass (stage a kernel, flux+update kernel)"}
+
+
+def oracle_setup(cfg_text):
+    """The oracle and the initial state of a workload, from the config text alone
+    (the oracle's own restatement of the mesh, coefficients and the seeded start;
+    nothing of the engine library is loaded)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    orc = pyoracle.Oracle.from_config(cfg_text)
+    return orc, pyoracle.to_ghosted(orc.initial_state())
 
 
 def describe(grid, precision):
@@ -116,18 +136,25 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def ncu_traffic(precision):
-    """DRAM bytes per flux launch from the committed ncu summary, if any."""
+def ncu_traffic(precision, grid):
+    """DRAM bytes per flux launch from the committed ncu capture of the same
+    grid and form (profiles/traffic.json, written from an ncu capture; ncu
+    cannot run inside this process), with the capture it comes from; None when
+    no capture of this grid exists."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         d = json.load(open(p))
-        return d.get(precision)
     except Exception:
-        return None
+        return None, None
+    e = d.get("flux", {}).get(precision)
+    if not e or list(e.get("grid_nx_ny_nz", [])) != list(grid):
+        return None, None
+    return e["dram_bytes"], {"source": "profiles/traffic.json (committed ncu capture, not measured in this run)",
+                             "kernel": e["kernel"], "command": d.get("command")}
 
 
 def fp64_inst_per_cell(kernel):
-    """FP64 thread instructions per cell of `kernel` from the committed ncu summary."""
+    """FP64 thread instructions per cell of `kernel` from the committed ncu capture."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         return json.load(open(p))["fp64_inst_per_cell"][kernel]
@@ -182,6 +209,7 @@ def run_form(args, precision, k, w):
         eng.run(1, w)
         eng.sync()
         ms, ms_a, ms_b = time_steps(eng, w + 1, k)
+        eng.sync()  # raises on a kernel-reported error (e.g. a timed-out TMA wait)
         n = grid[0] * grid[1] * grid[2]
         return n * k / (ms / 1e3) / 1e6, ms / k, ms_a / k, ms_b / k
 
@@ -189,17 +217,9 @@ def run_form(args, precision, k, w):
 def cpu_baseline(args, budget_s=12.0):
     """The oracle (CPU port of the reference step, OpenMP over all host cores) on
     the same workload; a bounded number of full-grid steps."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import pydugks
-    import pyoracle
     cfg, _, grid = workload(args, "fp64")
-    eng = pydugks.Engine(cfg)
-    f0 = eng.get_state()
-    xc, dxx = eng.mesh()
-    orc = pyoracle.Oracle.from_engine_info(eng.info, xc=xc, dxx=dxx)
-    eng.close()
-    g = pyoracle.to_ghosted(f0)
-    del f0
+    orc, g = oracle_setup(cfg)
+    import pyoracle
     threads = pyoracle.max_threads()
     t = time.perf_counter()
     orc.run(g, 1, 1, threads)
@@ -218,36 +238,28 @@ def other_configs(k=200, w=3, cpu_budget_s=3.0):
     """MLUPS of the other single-GPU workloads (they fit in L2, so MLUPS only):
     the laminar channel (32 x 64 x 32, walls at the wall-normal faces; in the
     reference orientation 64 wall-normal x 32 x 32) and the Taylor-Green vortex
-    (64^3 periodic, u0 = 0.05, Re = 1600), FP64 and FP32 on the GPU and the
-    oracle (FP64, OpenMP) on the host cores for a bounded number of steps."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import math
+    (64^3 periodic, u0 = 0.05 in the velocity and the density term, Re = 1600),
+    FP64 and FP32 on the GPU and the oracle (FP64, OpenMP) on the host cores for
+    a bounded number of steps."""
     import pydugks
-    import pyoracle
     import torch
-    L = 64 / (2 * math.pi)
-    cases = {
-        "laminar channel 32x64x32": dict(case="channel", nx=64, ny=32, nz=32, xwidth=64, ywidth=32, zwidth=32,
-                                         periods_x=0, CFL=0.5, visc=0.032, ambient_fz=6.25e-6),
-        "Taylor-Green 64^3": dict(case="tg_eq", nx=64, ny=64, nz=64, xwidth=64, ywidth=64, zwidth=64, periods_x=1,
-                                  CFL=0.5, visc=f"{0.05 * L / 1600:.9g}", ambient_fz=0.0),
-    }
+    import workloads
+    cases = {"laminar channel 32x64x32": workloads.laminar_config,
+             "Taylor-Green 64^3 u0=0.05 Re=1600": workloads.taylor_green_config}
     out = {}
-    for name, kw in cases.items():
+    for name, make in cases.items():
         res = {}
         for prec in ("fp64", "fp32"):
-            with pydugks.Engine(pydugks.make_config(precision=prec, **kw)) as eng:
+            with pydugks.Engine(make(precision=prec)) as eng:
                 eng.set_stream(torch.cuda.current_stream().cuda_stream)
                 eng.run(1, w)
                 eng.sync()
                 ms = time_steps(eng, w + 1, k)[0]
+                eng.sync()
                 res[prec + "_mlups"] = eng.nx * eng.ny * eng.nz * k / (ms / 1e3) / 1e6
-        with pydugks.Engine(pydugks.make_config(precision="fp64", **kw)) as eng:
-            f0 = eng.get_state()
-            xc, dxx = eng.mesh()
-            orc = pyoracle.Oracle.from_engine_info(eng.info, xc=xc, dxx=dxx)
-            n = eng.nx * eng.ny * eng.nz
-        g = pyoracle.to_ghosted(f0)
+        orc, g = oracle_setup(make(precision="fp64"))
+        import pyoracle
+        n = orc.cfg.nx * orc.cfg.ny * orc.cfg.nz
         threads = pyoracle.max_threads()
         t = time.perf_counter()
         orc.run(g, 1, 1, threads)
@@ -290,22 +302,18 @@ def reference_gpu(args, k=10):
 
 
 def main_reference(args):
+    """The reference arm: the reference step on the host cores.  The reference has
+    no CPU implementation of its step, so this is the oracle's restatement of it
+    (oracle/dugks_oracle.c, OpenMP over every host core), on the same workload
+    and config as the GPU arm; its mesh, coefficients and seeded initial state
+    come from the oracle's own restatement too, so the engine library is never
+    loaded by this arm."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import pydugks  # noqa: F401
+    cfg, meta, grid = workload(args, "fp64")
+    orc, g = oracle_setup(cfg)
     import pyoracle
-    cfg, _, grid = workload(args, "fp64")
-    # the initial state and mesh come from the same generator the GPU arm uses
-    eng = pydugks.Engine(cfg)
-    f0 = eng.get_state()
-    xc, dxx = eng.mesh()
-    orc = pyoracle.Oracle.from_engine_info(eng.info, xc=xc, dxx=dxx)
-    eng.close()
-    g = pyoracle.to_ghosted(f0)
-    del f0
     threads = pyoracle.max_threads()
     orc.run(g, 1, args.warmup, threads)
     t = time.perf_counter()
@@ -316,8 +324,7 @@ def main_reference(args):
     line = {"impl": "reference", "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": describe(grid, "fp64"), "grid": list(grid), "mesh": "tanh",
-                       "parallelism": "host OpenMP"},
+            "config": bench_config(args, meta, grid, world),
             "cpu_baseline": {"value": value, "unit": "MLUPS", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} full-grid FP64 steps after {args.warmup} warm-up steps; "
                                        "the reference has no CPU path, so this is the oracle's restatement of "
@@ -335,7 +342,6 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         return main_reference(args)
-    import numpy as np
     import torch
     import pydugks
     world, rank, local = dist_env()
@@ -360,6 +366,7 @@ def main():
     time.sleep(0.3)
     ms, ms_a, ms_b = time_steps(eng, W + 1, K)
     clocks = sampler.stop()
+    eng.sync()  # raises on a kernel-reported error (a timed-out TMA wait) instead of printing a number
     value, ms = combine_ranks(world, n, K, ms, dist, device="cuda")
 
     # end to end through the C ABI with host buffers: upload the state from
@@ -375,7 +382,8 @@ def main():
     for s in range(K):
         eng.step(W + K + 1 + s)
         eng.moments()
-    pydugks.lib().dg_get_state(eng._h, h_out.ctypes.data_as(pydugks._D))
+    eng._check(pydugks.lib().dg_get_state(eng._h, h_out.ctypes.data_as(pydugks._D)))
+    eng.sync()
     e2e_s = time.perf_counter() - t0
     e2e = {"value": n * K / e2e_s / 1e6, "unit": "MLUPS",
            "h2d_bytes_per_step": state_bytes / K,
@@ -387,8 +395,9 @@ def main():
     flux_bytes = 57 * info_bytes * n
     achieved = flux_bytes / (ms_b / K / 1e3) / 1e9
     peak, peak_kind = measured_peak_hbm()
+    traffic, traffic_src = ncu_traffic(args.precision, grid)
     roof = {"bound": "hbm", "kernel": "flux_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": ncu_traffic(args.precision),
+            "frac": achieved / peak, "traffic": traffic, "traffic_from": traffic_src,
             "peak_source": peak_kind, "alg_bytes_per_cell": 57 * info_bytes,
             "kernel_ms": {"fbar_kernel": ms_a / K, "flux_kernel": ms_b / K},
             "step_alg_bytes_per_cell": 95 * info_bytes,
@@ -431,10 +440,7 @@ def main():
                 "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": {"fp64": "f64", "fp32": "f32", "fp16": "f16-storage/f32", "bf16": "bf16-storage/f32"}[args.precision],
                 "data": "synthetic",
-                "config": {"workload": describe(grid, args.precision), "grid_nx_ny_nz": list(grid), "mesh": "tanh",
-                           "re_tau": 180, "nu": meta["nu"], "alpha": meta["alpha"], "parallelism": f"replicas x{world}",
-                           "l2": "inputs larger than L2 (f and f-bar-plus resident, %d MB each)" % (n * 19 * info_bytes // 2**20),
-                           "structure": "two-pass (stage a kernel, flux+update kernel)"},
+                "config": bench_config(args, meta, grid, world),
                 "e2e": e2e, "gpu_launches": (2 if args.precision == "fp32" else 3) * K, "roofline": roof, "clocks": clocks}
         line.update(extras)
         print(json.dumps(line), flush=True)

@@ -1313,10 +1313,12 @@ __device__ __forceinline__ unsigned smem_u32(const void *p)
     return static_cast<unsigned>(__cvta_generic_to_shared(p));
 }
 
-// bounded wait on an mbarrier phase; false if it never completed
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity)
+// bounded wait on an mbarrier phase; false if it did not complete within
+// `limit` polls (each try_wait may suspend the thread for a short,
+// hardware-defined time before it reports)
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int limit = 1 << 22)
 {
-    for (int it = 0; it < (1 << 22); ++it) {
+    for (int it = 0; it < limit; ++it) {
         unsigned ok;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -1457,6 +1459,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
     }
     // every plane issued (g <= ke) has been waited for: no bulk copy is left in flight
 }
+
 
 template <class T, class S, int W>
 constexpr size_t flux_tma_smem_bytes()

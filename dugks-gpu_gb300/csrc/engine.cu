@@ -117,6 +117,8 @@ struct dg_ctx {
     int recon = 0;          // 0 trilinear
     int stochastic = 1;     // 16-bit forms: stochastic rounding of the stored deviations
     double mesh_alpha = 0.85;
+    double xwidth_d = 0;    // xwidth parsed in double precision (stretched meshes)
+    double tg_u0 = 0.1;     // velocity amplitude of case=tg_eq (the reference's fixed 0.1 by default)
     std::string mesh_file;
     // derived
     int pitch = 0;
@@ -239,6 +241,11 @@ int load_config(dg_ctx *h, const ConfigFile &cf)
     else if (mesh == "file") h->mesh = 2;
     else return h->fail(DG_ERR_CONFIG, "config key 'mesh': expected uniform, tanh or file, got '" + mesh + "'");
     if (!cf.opt_double("mesh_alpha", 0.85, h->mesh_alpha, e)) return h->fail(DG_ERR_CONFIG, e);
+    // the stretched-mesh channel holds its width in double precision (a -r8
+    // parameter, src/fortran/channel/src/dugks.cuf:18); the mesh and its upper
+    // ghost use that value rather than the std::stof-rounded one
+    if (!cf.opt_double("xwidth", h->xwidth, h->xwidth_d, e)) return h->fail(DG_ERR_CONFIG, e);
+    if (!cf.opt_double("tg_u0", 0.1, h->tg_u0, e)) return h->fail(DG_ERR_CONFIG, e);
     h->mesh_file = cf.opt_string("mesh_file", "mesh.txt");
     const std::string rounding = cf.opt_string("rounding", "stochastic");
     if (rounding == "stochastic") h->stochastic = 1;
@@ -272,7 +279,7 @@ int build_mesh(dg_ctx *h)
     const int nx = h->nx;
     h->xf.assign(nx + 1, 0.0);
     if (h->mesh == 1) {
-        const double a = h->mesh_alpha, L = h->xwidth;
+        const double a = h->mesh_alpha, L = h->xwidth_d;
         if (!(a > 0 && a < 1)) return h->fail(DG_ERR_CONFIG, "mesh_alpha must lie in (0, 1)");
         for (int k = 0; k <= nx; ++k) {
             const double eta = -1. + 2. * ((k + 0) - 0.0) / nx;
@@ -296,7 +303,7 @@ int build_mesh(dg_ctx *h)
         if (!(h->dxx[i] > 0)) return h->fail(DG_ERR_CONFIG, "mesh faces must increase strictly");
     }
     h->xc[0] = -h->xc[1];
-    h->xc[nx + 1] = 2 * h->xwidth - h->xc[nx];
+    h->xc[nx + 1] = 2 * (h->mesh ? h->xwidth_d : h->xwidth) - h->xc[nx];
     h->dxx[0] = h->dxx[1];
     h->dxx[nx + 1] = h->dxx[nx];
     return DG_OK;
@@ -1083,7 +1090,9 @@ double feq_host(int p, double r, double u, double v, double w)
     return tp * r * (1.0 + eu + 0.5 * (eu * eu - uv));
 }
 
-// Initial state in dump order.  tg_eq / channel: src/dugks.cu:222-259.
+// Initial state in dump order.  tg_eq / channel: src/dugks.cu:222-259; the
+// tg_eq amplitude is the reference's 0.1 unless the extension key tg_u0 gives
+// another (it scales both the velocity and the density correction).
 // channel_turb (extension): laminar Poiseuille profile of bulk velocity
 // `ub` along the forcing axis plus seeded uniform perturbations and near-wall
 // streaks, f = feq(1, u).
@@ -1120,7 +1129,7 @@ int initial_state(dg_ctx *h, const ConfigFile &cf, std::vector<double> &f)
                 const double x = h->mesh ? h->xc[i] : (i - 0.5) * dx;
                 double rho = 1, u[3] = {0, 0, 0};
                 if (h->casename == "tg_eq") {
-                    const double vs = 0.1;
+                    const double vs = h->tg_u0;
                     rho = 1.0 + 1.0 * vs * vs / 16 * (std::cos(2 * pi2 / xwidth * x) + std::cos(2 * pi2 / ywidth * y)) *
                                     (std::cos(2 * pi2 / zwidth * z) + 2) / RT;
                     u[0] = vs * std::sin(pi2 / xwidth * x) * std::cos(pi2 / ywidth * y) * std::cos(pi2 / zwidth * z);
@@ -1424,8 +1433,22 @@ int dg_sync(dg_t *h)
     CK(cudaMemcpy(&flag, h->dev_err, sizeof(int), cudaMemcpyDeviceToHost), "error flag read");
     if (flag) {
         cudaMemset(h->dev_err, 0, sizeof(int));
-        return h->fail(DG_ERR_CUDA, "a TMA pipeline wait in the flux kernel timed out");
+        return h->fail(DG_ERR_CUDA, "a bounded device wait (the TMA pipeline of a flux or adjoint kernel) timed out");
     }
+    return DG_OK;
+}
+
+int dg_selftest_wait_timeout(dg_t *h, int limit, long long *waited_cycles)
+{
+    if (!h || limit < 1 || limit > (1 << 22)) return DG_ERR_ARG;
+    int rc = ensure_scratch(h, sizeof(long long));
+    if (rc) return rc;
+    long long *cyc = reinterpret_cast<long long *>(h->scratch);
+    CK(dg::launch_wait_timeout_selftest(h->dev_err, limit, cyc, h->stream), "wait time-out self-test launch");
+    long long c = 0;
+    CK(cudaMemcpyAsync(&c, cyc, sizeof(c), cudaMemcpyDeviceToHost, h->stream), "wait time-out self-test read");
+    CK(cudaStreamSynchronize(h->stream), "wait time-out self-test");
+    if (waited_cycles) *waited_cycles = c;
     return DG_OK;
 }
 

@@ -74,4 +74,8 @@ struct Kern {
 
 cudaError_t launch_stats_reduce(const double *partial, int nblocks, int nx, double *total, cudaStream_t st);
 
+// one thread waits `limit` polls on an mbarrier that nothing arrives at, then
+// raises *err (kern_fp64.cu); *polled_cycles = SM clock cycles spent waiting
+cudaError_t launch_wait_timeout_selftest(int *err, int limit, long long *polled_cycles, cudaStream_t st);
+
 }  // namespace dg

@@ -3,10 +3,9 @@
 // dg_stats_values (engine.cu) reduces the diag.dat / profiles-2.dat statistics
 // through a scratch buffer that the handle allocates with cudaMalloc on first
 // use.  Some callers cannot allocate device memory at the point where they
-// want statistics: code running inside CUDA stream capture (cudaMalloc is not
-// a capturable operation), host programs that hand all device memory to their
-// own pool or arena up front and forbid later allocations, and callers on a
-// memory budget that is already spent by the state arrays.  For them this file
+// want statistics: host programs that hand all device memory to their own
+// pool or arena up front and forbid later allocations, and callers whose
+// memory budget the state arrays have already spent.  For them this file
 // provides dg_stats_values_noalloc: the same reduction over an FP64 state that
 // the caller holds in device memory, with its scratch in a fixed
 // file-scope __device__ array instead of an allocation.

@@ -57,17 +57,14 @@ def main():
     import torch
     import dugks_autograd as da
 
-    n, u0s = args.n, 0.05
-    L = n / (2 * np.pi)
-    visc = u0s * L / 1600.0
-    # tg_eq builds the reference's TG field with amplitude 0.1; rescale the velocity to u0
-    cfg = pydugks.make_config(case="tg_eq", nx=n, ny=n, nz=n, xwidth=n, ywidth=n, zwidth=n, periods_x=1,
-                              CFL=0.5, visc=f"{visc:.9g}", ambient_fz=0.0, precision=args.precision)
+    n = args.n
+    # tg_eq with the amplitude u0 = 0.05 in the velocity and the density term (key tg_u0)
+    cfg = pydugks.taylor_green_config(n=n, u0=0.05, re=1600.0, precision=args.precision)
     eng = pydugks.Engine(cfg)
     f0 = eng.get_state()
     dt = torch.float64 if args.precision == "fp64" else torch.float32
     rho0, u_tg = da.macro(torch.from_numpy(f0).permute(3, 0, 1, 2).cuda())
-    u_init = (u_tg * (u0s / 0.1)).to(dt)
+    u_init = u_tg.to(dt)
     rho0 = rho0.to(dt)
 
     def J(u, every=args.every):
@@ -119,8 +116,7 @@ def main():
     Jfd, extra = J, {}
     if args.precision == "fp32":
         eng64 = pydugks.Engine(cfg.replace("precision=fp32", "precision=fp64"))
-        rho64, u_tg64 = da.macro(torch.from_numpy(eng64.get_state()).permute(3, 0, 1, 2).cuda())
-        u64 = u_tg64 * (u0s / 0.1)
+        rho64, u64 = da.macro(torch.from_numpy(eng64.get_state()).permute(3, 0, 1, 2).cuda())
 
         def Jfd(uu, every=args.every):
             f = da.feq(rho64, uu.double()).permute(1, 2, 3, 0)

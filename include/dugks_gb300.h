@@ -106,8 +106,20 @@ int dg_run(dg_t *h, int istep0, int nsteps);
  * launches in kernel_ms[0] and of the flux launches in kernel_ms[1]. */
 int dg_run_profiled(dg_t *h, int istep0, int nsteps, double *kernel_ms);
 
-/* Waits for the handle's stream and reports any pending CUDA error. */
+/* Waits for the handle's stream and reports any pending CUDA error, and
+ * DG_ERR_CUDA when a kernel gave up a bounded device wait (the TMA pipelines
+ * of the flux and adjoint kernels poll their mbarriers a bounded number of
+ * times, then raise a device flag and finish instead of hanging).  Reading the
+ * flag clears it. */
 int dg_sync(dg_t *h);
+
+/* Self-test of that time-out path (no counterpart in the reference): one
+ * kernel waits `limit` polls (1 .. 2^22) on an mbarrier that nothing arrives
+ * at -- no copy is issued, nothing is in flight -- raises the handle's device
+ * flag and returns.  Synchronous; the SM cycles spent waiting go to
+ * *waited_cycles (may be NULL).  The next dg_sync returns DG_ERR_CUDA and the
+ * handle stays usable. */
+int dg_selftest_wait_timeout(dg_t *h, int limit, long long *waited_cycles);
 
 /* --- macroscopic output and statistics --------------------------------- */
 
@@ -230,9 +242,9 @@ int dg_get_mesh(const dg_t *h, double *xc, double *dxx);
 
 /* The statistics of dg_stats_values (diag.dat and profiles-2.dat values) for
  * callers that cannot allocate device memory at the point where they need
- * them: code running under CUDA stream capture, where cudaMalloc is not
- * allowed, and host programs whose own allocator owns all device memory and
- * forbids later cudaMalloc calls.  This entry point allocates nothing; its
+ * them: host programs whose own allocator owns all device memory and forbids
+ * later cudaMalloc calls, and callers whose memory budget the state arrays
+ * have already spent.  This entry point allocates nothing; its
  * scratch is a fixed array in the library's device image (about 5 MB, present
  * on every GPU that loads the library until the process exits).
  *   f      FP64 state in device memory in the engine's SoA layout, e.g.
@@ -241,7 +253,10 @@ int dg_get_mesh(const dg_t *h, double *xc, double *dxx);
  *   hdt, fx, fy, fz   the velocity shift hdt*F of the macro output
  *   out    device array of 12 + 9*nx + 1 doubles: the 12 diag values, the
  *          nx x 9 profile values, then the number of cells with a non-finite
- *          moment
+ *          moment (dg_stats_values returns DG_ERR_NUMERIC for such a state;
+ *          here the caller reads the count)
+ * Only FP64 data is valid input: the pointer carries no type, and the state of
+ * an fp32 or 16-bit engine gives meaningless numbers.
  * Asynchronous on `stream` (a cudaStream_t; 0 = legacy default stream).
  * The first call on a device looks up the scratch array's device address with
  * that device current; make that first call before any stream capture.  All
@@ -251,6 +266,8 @@ int dg_get_mesh(const dg_t *h, double *xc, double *dxx);
  * last failure is dg_noalloc_last_error(). */
 int dg_stats_values_noalloc(const double *f, int nx, int ny, int nz, int pitch, long long pop_stride,
                             double hdt, double fx, double fy, double fz, double *out, void *stream);
+/* Message of the last failing dg_stats_values_noalloc call made by the
+ * calling host thread (the message buffer is per thread). */
 const char *dg_noalloc_last_error(void);
 
 #ifdef __cplusplus

@@ -29,6 +29,7 @@ typedef struct {
 
 int oracle_coefficients_f64(const oracle_cfg *c, double *out13);
 int oracle_init_f64(const oracle_cfg *c, int kind, double *f);
+int oracle_init_case_f64(const oracle_cfg *c, int kind, const double *par, double *f);
 int oracle_fbar_f64(const oracle_cfg *c, const double *f, double *fb, int step, int nthreads);
 int oracle_run_f64(const oracle_cfg *c, double *f, int istep0, int nsteps, int nthreads);
 int oracle_macro_f64(const oracle_cfg *c, const double *f, double *rho, double *ux, double *uy, double *uz);
@@ -37,6 +38,7 @@ int oracle_stats_f64(int nx, int ny, int nz, const double *rhg, const double *ux
 
 int oracle_coefficients_f32(const oracle_cfg *c, double *out13);
 int oracle_init_f32(const oracle_cfg *c, int kind, float *f);
+int oracle_init_case_f32(const oracle_cfg *c, int kind, const double *par, float *f);
 int oracle_fbar_f32(const oracle_cfg *c, const float *f, float *fb, int step, int nthreads);
 int oracle_run_f32(const oracle_cfg *c, float *f, int istep0, int nsteps, int nthreads);
 int oracle_macro_f32(const oracle_cfg *c, const float *f, float *rho, float *ux, float *uy, float *uz);

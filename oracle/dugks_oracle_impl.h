@@ -136,6 +136,92 @@ int FN(oracle_init)(const oracle_cfg *c, int kind, REAL *f)
     return 0;
 }
 
+/* splitmix64 finaliser and the uniform value in [-1, 1) of (seed, cell,
+ * component) that defines the seeded synthetic channel start: the 53 high bits
+ * of splitmix64(seed*0xD1B54A32D192ED03 + 3*cell + component). */
+static inline unsigned long long FN(smix)(unsigned long long z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static inline double FN(usym)(unsigned long long seed, unsigned long long cell, int comp)
+{
+    const unsigned long long z = FN(smix)(seed * 0xD1B54A32D192ED03ull + cell * 3ull + (unsigned long long)comp);
+    return (double)(z >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+}
+
+/* Initial states by case, interior cells of the ghosted box (ghosts untouched).
+ *   kind 0  tg_eq (src/dugks.cu:222-238) with the amplitude par[0] in place of
+ *           the reference's fixed 0.1, in the velocity and the density term;
+ *   kind 1  channel (src/dugks.cu:239-255);
+ *   kind 2  the seeded turbulent-channel start of the benchmark workloads (no
+ *           counterpart in the reference, whose channel restarts from a DNS
+ *           dump): along the streamwise axis a (the largest ambient force
+ *           component) the laminar profile 6 ub eta (1 - eta), eta = x/xwidth,
+ *           x the cell centre (c->xc on a stretched mesh); on every component
+ *           amp*ub*usym(seed, cell, component); along a the near-wall streaks
+ *           streak*ub*sin(2 pi m s) e exp(1 - e), e = y+/10 = min(x, xwidth - x)
+ *           re_tau/(xwidth/2)/10, s = the spanwise coordinate / its width (y
+ *           when a = z, else z).  par = {ub, re_tau, amp, streak, seed, m}.
+ * f = feq(rho, u) with the host equilibrium (src/dugks.cu:304-309). */
+int FN(oracle_init_case)(const oracle_cfg *c, int kind, const double *par, REAL *f)
+{
+    const int nx = c->nx, ny = c->ny, nz = c->nz;
+    FN(coef_t) q;
+    const double pi = 3.141592653589793, pi2 = 2 * pi;
+    int i, j, k, ip;
+    int sa = 2;
+    FN(make_coef)(c, &q);
+    (void)q;
+    if (kind < 0 || kind > 2) return -1;
+    const double Fa[3] = {c->Fx, c->Fy, c->Fz};
+    if (fabs(Fa[0]) > fabs(Fa[sa])) sa = 0;
+    if (fabs(Fa[1]) > fabs(Fa[sa])) sa = 1;
+    for (k = 1; k <= nz; k++) {
+        const double z = (k - 0.5) * c->dz;
+        for (j = 1; j <= ny; j++) {
+            const double y = (j - 0.5) * c->dy;
+            for (i = 1; i <= nx; i++) {
+                const double x = c->mesh == 1 ? c->xc[i] : (i - 0.5) * c->dx;
+                double rho = 1, u[3] = {0, 0, 0};
+                if (kind == 0) {
+                    const double vs = par[0];
+                    rho = 1.0 + 1.0 * vs * vs / 16 * (cos(2 * pi2 / c->xwidth * x) + cos(2 * pi2 / c->ywidth * y)) *
+                                    (cos(2 * pi2 / c->zwidth * z) + 2) / (1. / 3.);
+                    u[0] = vs * sin(pi2 / c->xwidth * x) * cos(pi2 / c->ywidth * y) * cos(pi2 / c->zwidth * z);
+                    u[1] = -vs * cos(pi2 / c->xwidth * x) * sin(pi2 / c->ywidth * y) * cos(pi2 / c->zwidth * z);
+                } else if (kind == 1) {
+                    u[2] = 0.1;
+                } else {
+                    const double ub = par[0], re_tau = par[1], amp = par[2], streak = par[3];
+                    const unsigned long long seed = (unsigned long long)par[4];
+                    const int m = (int)par[5];
+                    const unsigned long long cell = ((unsigned long long)(k - 1) * ny + (j - 1)) * nx + (i - 1);
+                    const double eta = x / c->xwidth, H = 0.5 * c->xwidth;
+                    const double wall = x < c->xwidth - x ? x : c->xwidth - x;
+                    const double e = wall * (re_tau / H) / 10.0;
+                    const double s = sa == 2 ? y / c->ywidth : z / c->zwidth;
+                    int a;
+                    u[sa] = 6.0 * ub * eta * (1 - eta);
+                    for (a = 0; a < 3; a++) u[a] += amp * ub * FN(usym)(seed, cell, a);
+                    u[sa] += streak * ub * sin(pi2 * m * s) * e * exp(1 - e);
+                }
+                for (ip = 0; ip < 19; ip++) {
+                    const double RT = 1. / 3.;
+                    const double tp = ip == 0 ? 1.0 / 3.0 : (ip <= 6 ? 1.0 / 18.0 : 1.0 / 36.0);
+                    const double eu = (CIX[ip] * u[0] + CIY[ip] * u[1] + CIZ[ip] * u[2]) / RT;
+                    const double uv = (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]) / RT;
+                    f[IDX(ip, i, j, k)] = (REAL)(tp * rho * (1.0 + eu + 0.5 * (eu * eu - uv)));
+                }
+            }
+        }
+    }
+    return 0;
+}
+
 /* Per-cell body force, src/dugks.cu:1066-1126 (calc_force / calc_perturb_force).
  * Writes interior cells of the three ghosted force arrays. */
 static void FN(force_field)(const oracle_cfg *c, const FN(coef_t) *q, int step, REAL *fxa, REAL *fya, REAL *fza)

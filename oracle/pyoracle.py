@@ -45,6 +45,7 @@ def lib():
         for sfx, T in (("f64", _D), ("f32", _F)):
             getattr(L, f"oracle_coefficients_{sfx}").argtypes = [P, _D]
             getattr(L, f"oracle_init_{sfx}").argtypes = [P, ctypes.c_int, T]
+            getattr(L, f"oracle_init_case_{sfx}").argtypes = [P, ctypes.c_int, _D, T]
             getattr(L, f"oracle_fbar_{sfx}").argtypes = [P, T, T, ctypes.c_int, ctypes.c_int]
             getattr(L, f"oracle_run_{sfx}").argtypes = [P, T, ctypes.c_int, ctypes.c_int, ctypes.c_int]
             getattr(L, f"oracle_macro_{sfx}").argtypes = [P, T, T, T, T, T]
@@ -82,6 +83,38 @@ class Oracle:
         self.shape = (nz + 2, ny + 2, nx + 2, 19)
 
     @classmethod
+    def from_config(cls, text, dtype=np.float64, workdir=".", **kw):
+        """The oracle of a config.txt text, set up from the text alone (nothing
+        of the engine): reference keys parsed as src/config.h and
+        src/numerics.cu:62-106 do (std::stof / std::stoi), dx, dy, dz and dt in
+        the reference's `real`, and for the extension key mesh=tanh|file the
+        stretched mesh of src/fortran/channel (faces from run/mesh.py:21-25 or
+        from the mesh file, centres, widths and ghosts as dugks.cuf:107-121,
+        dt from the first cell width as dugks.cuf:138)."""
+        c = setup_from_config(text, dtype=dtype, workdir=workdir)
+        kw.setdefault("recon", 1 if c["kv"].get("recon") == "gradient" else 0)
+        o = cls(c["nx"], c["ny"], c["nz"], c["dx"], c["dy"], c["dz"], c["dt"], c["visc"], F=c["F"],
+                periodic_x=c["periodic_x"], xwidth=c["xwidth"], ywidth=c["ywidth"], zwidth=c["zwidth"],
+                xc=c["xc"], dxx=c["dxx"], perturb=c["perturb"], dtype=dtype, **kw)
+        o.setup = c
+        return o
+
+    def initial_state(self):
+        """Initial state (dump order) of the case the config names: tg_eq (with the
+        extension key tg_u0), channel, or the seeded channel_turb start."""
+        c = self.setup
+        kv = c["kv"]
+        kind = self.CASE_KIND[c["case"]]
+        if kind == 0:
+            par = (_double(kv.get("tg_u0", "0.1")),)
+        elif kind == 2:
+            par = (_double(kv.get("ub", "0.1")), _double(kv.get("re_tau", "180")), _double(kv.get("pert_amp", "0.1")),
+                   _double(kv.get("streak_amp", "0.05")), _stoi(kv.get("seed", "0")), _stoi(kv.get("streak_m", "4")))
+        else:
+            par = ()
+        return interior(self.init_case(kind, par))
+
+    @classmethod
     def from_engine_info(cls, info, xc=None, dxx=None, dtype=np.float64, **kw):
         F = tuple(info.ambient)
         return cls(info.nx, info.ny, info.nz, info.dx, info.dy, info.dz, info.dt, info.visc, F=F,
@@ -101,6 +134,20 @@ class Oracle:
     def init(self, kind):
         f = np.zeros(self.shape, dtype=self.dtype)
         rc = getattr(lib(), f"oracle_init_{self.sfx}")(ctypes.byref(self.cfg), kind, self._p(f))
+        assert rc == 0
+        return f
+
+    CASE_KIND = {"tg_eq": 0, "channel": 1, "channel_turb": 2}
+
+    def init_case(self, kind, par=()):
+        """Initial state of case `kind` (0 tg_eq with amplitude par[0], 1 channel,
+        2 the seeded turbulent-channel start, par = (ub, re_tau, amp, streak, seed, m))
+        on the interior of a ghosted box."""
+        f = np.zeros(self.shape, dtype=self.dtype)
+        p = np.zeros(8)
+        p[:len(par)] = par
+        rc = getattr(lib(), f"oracle_init_case_{self.sfx}")(ctypes.byref(self.cfg), kind, p.ctypes.data_as(_D),
+                                                           self._p(f))
         assert rc == 0
         return f
 
@@ -131,6 +178,103 @@ class Oracle:
                                                    self._p(ux), self._p(uy), self._p(uz),
                                                    diag.ctypes.data_as(_D), prof.ctypes.data_as(_D))
         return diag, prof
+
+
+# ---------------------------------------------------------------------------
+# configuration and mesh, restated from the reference (independent of the engine)
+# ---------------------------------------------------------------------------
+_libc = None
+
+
+def _c():
+    global _libc
+    if _libc is None:
+        _libc = ctypes.CDLL(None)
+        _libc.strtof.restype = ctypes.c_float
+        _libc.strtof.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p)]
+        _libc.strtod.restype = ctypes.c_double
+        _libc.strtod.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p)]
+        _libc.strtol.restype = ctypes.c_long
+        _libc.strtol.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_char_p), ctypes.c_int]
+    return _libc
+
+
+def _stof(v):
+    """std::stof (strtof: the value rounded to float once), widened."""
+    return float(_c().strtof(v.encode(), None))
+
+
+def _double(v):
+    return float(_c().strtod(v.encode(), None))
+
+
+def _stoi(v):
+    return int(_c().strtol(v.encode(), None, 10))
+
+
+def parse_config(text):
+    """key -> value of config.txt text with src/config.h:17-74's rules: lines split
+    at '=', the second field is the value, lines without '=' are ignored, no
+    trimming, the first occurrence of a key wins."""
+    kv = {}
+    for line in text.split("\n"):
+        parts = line.split("=")
+        if len(parts) > 1 and parts[0] not in kv:
+            kv[parts[0]] = parts[1]
+    return kv
+
+
+def tanh_faces(nx, L, alpha):
+    """nx+1 face positions of the tanh wall-normal mesh, src/fortran/channel/run/mesh.py:21-25."""
+    eta = -1.0 + 2.0 * np.arange(nx + 1, dtype=np.float64) / nx
+    return L / (2.0 * alpha) * np.tanh(eta * 0.5 * (np.log(1.0 + alpha) - np.log(1.0 - alpha))) + 0.5 * L
+
+
+def mesh_from_faces(xf, xwidth):
+    """Cell centres and widths 0..nx+1 with the mirrored ghosts,
+    src/fortran/channel/src/dugks.cuf:114-121."""
+    xf = np.asarray(xf, dtype=np.float64)
+    nx = len(xf) - 1
+    xc = np.zeros(nx + 2)
+    dxx = np.zeros(nx + 2)
+    xc[1:nx + 1] = 0.5 * (xf[1:] + xf[:-1])
+    dxx[1:nx + 1] = xf[1:] - xf[:-1]
+    xc[0] = -xc[1]
+    xc[nx + 1] = 2 * xwidth - xc[nx]
+    dxx[0] = dxx[1]
+    dxx[nx + 1] = dxx[nx]
+    return xc, dxx
+
+
+def setup_from_config(text, dtype=np.float64, workdir="."):
+    """Grid, coefficients and mesh of a config text, computed here from the
+    reference's formulas (src/numerics.cu:74-105 in `real` = dtype;
+    the stretched mesh in double precision as the -r8 Fortran channel)."""
+    kv = parse_config(text)
+    R = np.float64 if np.dtype(dtype) == np.float64 else np.float32
+    nx, ny, nz = (_stoi(kv[k]) for k in ("nx", "ny", "nz"))
+    cfl, xw, yw, zw, visc = (R(_stof(kv[k])) for k in ("CFL", "xwidth", "ywidth", "zwidth", "visc"))
+    F = tuple(float(R(_stof(kv[k]))) for k in ("ambient_fx", "ambient_fy", "ambient_fz"))
+    RT = R(1.0 / 3.0)
+    dx, dy, dz = xw / R(nx), yw / R(ny), zw / R(nz)
+    mesh = kv.get("mesh", "uniform")
+    xc = dxx = None
+    if mesh in ("tanh", "file"):
+        xw_d = _double(kv["xwidth"])
+        if mesh == "tanh":
+            xf = tanh_faces(nx, xw_d, _double(kv.get("mesh_alpha", "0.85")))
+        else:
+            path = kv.get("mesh_file", "mesh.txt")
+            if not os.path.isabs(path):
+                path = os.path.join(workdir, path)
+            xf = np.array(open(path).read().split()[:nx + 1], dtype=np.float64)
+        xc, dxx = mesh_from_faces(xf, xw_d)
+        dt = cfl * R(dxx[1]) / np.sqrt(R(6) * RT)
+    else:
+        dt = cfl * dx / np.sqrt(R(6) * RT)
+    return dict(kv=kv, case=kv["case"], nx=nx, ny=ny, nz=nz, dx=float(dx), dy=float(dy), dz=float(dz),
+                dt=float(dt), visc=float(visc), F=F, xwidth=float(xw), ywidth=float(yw), zwidth=float(zw),
+                periodic_x=_stoi(kv["periods_x"]), perturb=_stoi(kv["perturb"]), xc=xc, dxx=dxx)
 
 
 def to_ghosted(f_dump, dtype=np.float64):

@@ -29,10 +29,12 @@ def make_pair(name, precision="fp64", seed=1, workdir=".", **over):
     kw = dict(CASES[name])
     kw.update(over)
     kw["precision"] = precision
-    eng = pydugks.Engine(pydugks.make_config(**kw), workdir=workdir)
-    xc, dxx = eng.mesh()
+    cfg = pydugks.make_config(**kw)
+    eng = pydugks.Engine(cfg, workdir=workdir)
     dtype = np.float64 if precision == "fp64" else np.float32
-    orc = pyoracle.Oracle.from_engine_info(eng.info, xc=xc, dxx=dxx, dtype=dtype)
+    # the oracle is set up from the config text alone (mesh, dt and coefficients
+    # restated from the reference), never from the engine's own tables
+    orc = pyoracle.Oracle.from_config(cfg, dtype=dtype, workdir=workdir)
     f0 = seeded_state(eng.nx, eng.ny, eng.nz, seed=seed)
     eng.set_state(f0)
     return eng, orc, f0

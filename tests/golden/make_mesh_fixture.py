@@ -1,13 +1,15 @@
 """Copies the reference's tanh mesh (src/fortran/channel/run/mesh.txt: 129 face
 positions for nx=128, zsize=61.72, alpha=0.85, written by run/mesh.py) into
 tests/golden/mesh_tanh_128.txt as a golden vector for the engine's mesh
-generator.  Run here, where the reference is mounted:
-    python tests/golden/make_mesh_fixture.py /root/reference
+generator.  Run where the reference is mounted, with its root as the argument:
+    python tests/golden/make_mesh_fixture.py REFERENCE_ROOT
 """
 import os
 import sys
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_mesh_fixture.py REFERENCE_ROOT")
+ref = sys.argv[1]
 src = os.path.join(ref, "src/fortran/channel/run/mesh.txt")
 vals = [float(l) for l in open(src) if l.strip()]
 assert len(vals) == 129

@@ -47,8 +47,9 @@ def test_gradient_reconstruction_matches_oracle(case):
     from seeded import seeded_state
     kw = dict(C[case])
     kw["recon"] = "gradient"
-    eng = pydugks.Engine(pydugks.make_config(**kw))
-    orc = pyoracle.Oracle.from_engine_info(eng.info, recon=1)
+    cfg = pydugks.make_config(**kw)
+    eng = pydugks.Engine(cfg)
+    orc = pyoracle.Oracle.from_config(cfg)
     f0 = seeded_state(eng.nx, eng.ny, eng.nz, seed=3)
     eng.set_state(f0)
     got, want = run_both(eng, orc, f0, 1, 20)
@@ -68,8 +69,9 @@ def test_gradient_reconstruction_fp32_matches_oracle(case):
     kw = dict(C[case])
     kw["recon"] = "gradient"
     kw["precision"] = "fp32"
-    eng = pydugks.Engine(pydugks.make_config(**kw))
-    orc = pyoracle.Oracle.from_engine_info(eng.info, recon=1, dtype=np.float32)
+    cfg = pydugks.make_config(**kw)
+    eng = pydugks.Engine(cfg)
+    orc = pyoracle.Oracle.from_config(cfg, dtype=np.float32)
     f0 = seeded_state(eng.nx, eng.ny, eng.nz, seed=3)
     eng.set_state(f0)
     got, want = run_both(eng, orc, f0, 1, 20)
@@ -90,7 +92,7 @@ def test_edge_shapes_match_oracle(shape, periodic_x):
     cfg = pydugks.make_config(nx=nx, ny=ny, nz=nz, xwidth=nx, ywidth=ny, zwidth=nz, periods_x=periodic_x,
                               CFL=0.5, visc=0.02, ambient_fx=1e-5 if periodic_x else 0.0, ambient_fz=1e-5)
     eng = pydugks.Engine(cfg)
-    orc = pyoracle.Oracle.from_engine_info(eng.info)
+    orc = pyoracle.Oracle.from_config(cfg)
     f0 = seeded_state(nx, ny, nz, seed=9)
     eng.set_state(f0)
     got, want = run_both(eng, orc, f0, 1, 10)

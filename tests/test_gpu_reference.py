@@ -48,7 +48,7 @@ def test_oracle_and_engine_match_reference_fp64(case, nsteps):
     eng.set_state(f0)
     eng.run(1, nsteps)
     got = eng.get_state()
-    orc = pyoracle.Oracle.from_engine_info(eng.info)
+    orc = pyoracle.Oracle.from_config(pydugks.make_config(**kw))
     g = pyoracle.to_ghosted(f0)
     orc.run(g, 1, nsteps)
     e_oracle = rel_err(pyoracle.interior(g), pyoracle.interior(ref))
@@ -80,8 +80,9 @@ def test_gradient_option_matches_reference():
     f0 = seeded_state(kw["nx"], kw["ny"], kw["nz"], seed=5)
     ref = pyoracle.to_ghosted(f0)
     pyoracle.ref_run(ref, **_ref_args(kw), istep0=1, nsteps=5, prec=0, recon=1)
-    eng = pydugks.Engine(pydugks.make_config(recon="gradient", **kw))
-    orc = pyoracle.Oracle.from_engine_info(eng.info, recon=1)
+    cfg = pydugks.make_config(recon="gradient", **kw)
+    eng = pydugks.Engine(cfg)
+    orc = pyoracle.Oracle.from_config(cfg)
     g = pyoracle.to_ghosted(f0)
     orc.run(g, 1, 5)
     assert rel_err(pyoracle.interior(g), pyoracle.interior(ref)) <= 1e-13

@@ -17,10 +17,13 @@ from seeded import seeded_state, rel_err  # noqa: E402
 NX, NY, NZ = 258, 197, 131
 
 
+def _config(prec, nz=NZ):
+    return pydugks.make_config(nx=NX, ny=NY, nz=nz, xwidth=NX, ywidth=NY, zwidth=nz, periods_x=0, CFL=0.5,
+                               visc=0.02, ambient_fz=1e-5, precision=prec)
+
+
 def _engine(prec, nz=NZ):
-    cfg = pydugks.make_config(nx=NX, ny=NY, nz=nz, xwidth=NX, ywidth=NY, zwidth=nz, periods_x=0, CFL=0.5,
-                              visc=0.02, ambient_fz=1e-5, precision=prec)
-    return pydugks.Engine(cfg)
+    return pydugks.Engine(_config(prec, nz))
 
 
 def test_forms_agree_on_a_large_ragged_grid():
@@ -47,8 +50,7 @@ def test_fp64_large_slab_matches_oracle():
     import pyoracle
     nz = 4
     eng = _engine("fp64", nz=nz)
-    xc, dxx = eng.mesh()
-    orc = pyoracle.Oracle.from_engine_info(eng.info, xc=xc, dxx=dxx)
+    orc = pyoracle.Oracle.from_config(_config("fp64", nz))
     f0 = seeded_state(NX, NY, nz, seed=13)
     eng.set_state(f0)
     eng.run(1, 2)

@@ -1,10 +1,11 @@
 """The allocation-free statistics entry point (dg_stats_values_noalloc).
 
 It exists for callers that cannot allocate device memory when they ask for
-statistics -- code under CUDA stream capture, or hosts whose own allocator
-owns the device memory -- and keeps its scratch in a fixed array of the
-library instead.  It must give the statistics of dg_stats_values (the entry
-point that allocates its scratch) on the same state, within the tolerance of
+statistics -- hosts whose own allocator owns all of the device memory, or
+whose memory budget the state arrays have already spent -- and keeps its
+scratch in a fixed array of the library instead.  It must give the statistics
+of dg_stats_values (the entry point that allocates its scratch) on the same
+state, within the tolerance of
 tests/test_gpu_parity.py::test_stats_match_oracle, call after call: the state
 changes between the two calls checked here, so a stale scratch array would
 show.  Collected last so that a failure here leaves the rest of a -x run done.
@@ -20,7 +21,7 @@ torch = pytest.importorskip("torch")
 
 import pydugks  # noqa: E402
 from _cases import make_pair  # noqa: E402
-from seeded import rel_err  # noqa: E402
+from seeded import rel_err, seeded_state  # noqa: E402
 
 TOL = 1e-13
 
@@ -50,6 +51,30 @@ def test_noalloc_statistics_equal_the_allocating_entry_point_on_two_calls_in_a_r
         assert bad == 0
         assert rel_err(diag, diag_ref) <= TOL, call
         assert np.max(np.abs(prof - prof_ref)) <= TOL * max(1.0, np.max(np.abs(prof_ref))), call
+
+
+def test_noalloc_statistics_at_the_largest_accepted_nx():
+    """nx = 512 (two x blocks of the first pass, the most scratch) with ny*nz = 128
+    rows, more than the 64 row blocks, so every block sums several rows."""
+    cfg = pydugks.make_config(nx=512, ny=16, nz=8, xwidth=512, ywidth=16, zwidth=8, periods_x=0, CFL=0.5,
+                              visc=0.02, ambient_fz=1e-5)
+    eng = pydugks.Engine(cfg)
+    eng.set_state(seeded_state(512, 16, 8, seed=21))
+    stream = torch.cuda.current_stream().cuda_stream
+    eng.set_stream(stream)
+    nx = eng.nx
+    out = torch.full((12 + 9 * nx + 1,), float("nan"), dtype=torch.float64, device="cuda")
+    for call in range(2):
+        eng.run(1 + 3 * call, 3)
+        diag_ref, prof_ref = eng.stats_values()
+        _noalloc(eng, out, stream)
+        torch.cuda.synchronize()
+        o = out.cpu().numpy()
+        diag, prof, bad = o[:12], o[12:12 + 9 * nx].reshape(nx, 9), o[12 + 9 * nx]
+        assert bad == 0
+        assert rel_err(diag, diag_ref) <= TOL, call
+        assert np.max(np.abs(prof - prof_ref)) <= TOL * max(1.0, np.max(np.abs(prof_ref))), call
+    eng.close()
 
 
 def test_noalloc_rejects_grids_beyond_its_maximum():
