@@ -336,9 +336,13 @@ __global__ void __launch_bounds__(32 * W, MINB) adj_faces_tma_kernel(const __gri
         }
     };
     unsigned phase = 0;
+    int wait_limit = kWaitPolls;
     auto wait = [&](int g) {
         const int s = g & 3;
-        if (!mbar_wait(smem_u32(mbar + s), (phase >> s) & 1u)) atomicOr(P.err, 1);
+        if (!mbar_wait(smem_u32(mbar + s), (phase >> s) & 1u, wait_limit)) {
+            atomicOr(P.err, 1);
+            wait_limit = kWaitPollsAfterFailure;
+        }
         phase ^= 1u << s;
     };
 

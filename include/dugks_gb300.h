@@ -114,7 +114,7 @@ int dg_run_profiled(dg_t *h, int istep0, int nsteps, double *kernel_ms);
 int dg_sync(dg_t *h);
 
 /* Self-test of that time-out path (no counterpart in the reference): one
- * kernel waits `limit` polls (1 .. 2^22) on an mbarrier that nothing arrives
+ * kernel waits `limit` polls (1 .. 2^22; the pipelines use 2^18) on an mbarrier that nothing arrives
  * at -- no copy is issued, nothing is in flight -- raises the handle's device
  * flag and returns.  Synchronous; the SM cycles spent waiting go to
  * *waited_cycles (may be NULL).  The next dg_sync returns DG_ERR_CUDA and the

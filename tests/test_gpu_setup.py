@@ -8,7 +8,8 @@ of the benchmark workloads).
 
 Tolerances: mesh centres and widths bit-identical for a mesh file (the same
 two operations on the same doubles), 1e-12 absolute for the tanh generator
-(libm tanh/log against numpy's); time step and coefficients bit-identical;
+(libm tanh/log against numpy's); time step and coefficients bit-identical
+(1e-13 relative on a tanh mesh, where dt follows the first cell width);
 initial states 1e-15 relative (the same double expressions, libm against
 libm).
 """
@@ -98,13 +99,16 @@ def test_time_step_and_coefficients_equal_the_oracle(name):
     cfg = _configs()[name]
     dtype = np.float32 if "precision=fp32" in cfg else np.float64
     orc = pyoracle.Oracle.from_config(cfg, dtype=dtype)
+    # on a tanh mesh dt comes from the first cell width, which libm's tanh and
+    # numpy's give to the last few bits (1e-13 relative); otherwise bit-identical
+    rtol = 1e-13 if orc.setup["xc"] is not None else 0.0
     with pydugks.Engine(cfg) as eng:
         info = eng.info
         for key in ("dx", "dy", "dz", "dt"):
-            assert getattr(info, key) == orc.setup[key], key
+            assert abs(getattr(info, key) - orc.setup[key]) <= rtol * abs(orc.setup[key]), key
         coef = orc.coefficients()  # visc RT hdt bw0 bw1 bw2 fw0 fw1 fw2 dx dy dz dt
         for key, idx in (("bw0", 3), ("bw1", 4), ("bw2", 5), ("fw0", 6), ("fw1", 7), ("fw2", 8)):
-            assert getattr(info, key) == coef[idx], key
+            assert abs(getattr(info, key) - coef[idx]) <= rtol * abs(coef[idx]), key
         if orc.setup["xc"] is not None:
             xc, dxx = eng.mesh()
             assert np.max(np.abs(xc - orc.setup["xc"])) <= 1e-12
@@ -147,5 +151,5 @@ def test_tg_amplitude_scales_velocity_and_density():
         rho = f.sum(-1)
         jx = (f * np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1, 0, 0, 0, 0])).sum(-1)
         states[u0] = (rho - 1.0, jx / rho)
-    assert np.allclose(states[0.05][0], states[0.1][0] / 4, rtol=1e-12, atol=1e-16)
-    assert np.allclose(states[0.05][1], states[0.1][1] / 2, rtol=1e-12, atol=1e-16)
+    assert np.allclose(states[0.05][0], states[0.1][0] / 4, rtol=1e-12, atol=1e-14)
+    assert np.allclose(states[0.05][1], states[0.1][1] / 2, rtol=1e-12, atol=1e-14)
