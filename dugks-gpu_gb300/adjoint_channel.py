@@ -98,10 +98,18 @@ def gradient_run(torch, da, args):
     (g,) = torch.autograd.grad(J, [phi])
     torch.cuda.synchronize()
     t2 = time.perf_counter()
+    # the same gradient once more with every action bracketed by CUDA events: GPU time per kind
+    eng.field_grad(reset=True)
+    da.PROFILE = da.ActionTimer()
+    _, Jp = da.run_objective(f0, phi, eng, 1, args.steps, obj, snaps=snaps, axis=2)
+    torch.autograd.grad(Jp, [phi])
+    breakdown = {k: {"count": c, "gpu_ms": round(ms, 1)} for k, (c, ms) in da.PROFILE.summary().items()}
+    da.PROFILE = None
     gd = g.double()
     res = dict(J=float(J.detach()), tau_w_laminar=meta["utau"] ** 2, snaps=snaps, snap_gb=round(peak * state_bytes / 1e9, 2),
                recomputed_steps=total_adv - spine_adv,
                forward_sweep_s=round(t1 - t0, 3), backward_s=round(t2 - t1, 3),
+               gpu_ms_by_action=breakdown,
                adjoint_ms_per_step_harness=(t2 - t1) * 1e3 / args.steps,
                grad_l2=float(gd.norm()), grad_max=float(gd.abs().max()),
                grad_sum=float(gd.sum()), grad_mean_wall_cells=float(gd[:, :, [0, -1]].mean()),
@@ -171,6 +179,10 @@ def main():
                adjoint_over_forward=adj_ms / fwd32f, adjoint_over_plain_forward=adj_ms / fwd32,
                gradient_ms_per_step=grad["adjoint_ms_per_step_harness"] + grad["forward_sweep_s"] * 1e3 / args.steps,
                **grad)
+    # the adjoint cost per step: the whole gradient (forward sweep, recomputation, adjoint) per step
+    # and the reversal alone, each over the forward step it differentiates
+    res["gradient_over_forward_step"] = res["gradient_ms_per_step"] / fwd32f
+    res["reversal_over_forward_step"] = res["adjoint_ms_per_step_harness"] / fwd32f
     if args.fd_steps:
         res["fd_fp64"] = fd_check(torch, da, args)
     print(json.dumps(res))

@@ -68,6 +68,35 @@ def _sync_stream(eng):
     eng.set_stream(torch.cuda.current_stream().cuda_stream)
 
 
+class ActionTimer:
+    """GPU time per kind of action of a checkpointed reversal (CUDA events on the
+    current stream).  Assign an instance to `dugks_autograd.PROFILE` to have
+    DugksObjectiveRun record into it; `summary()` synchronises once and gives
+    {kind: (count, milliseconds)}."""
+
+    def __init__(self):
+        self.events = {}
+
+    def wrap(self, kind, fn, *a):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = fn(*a)
+        e1.record()
+        self.events.setdefault(kind, []).append((e0, e1))
+        return out
+
+    def summary(self):
+        torch.cuda.synchronize()
+        return {k: (len(v), sum(a.elapsed_time(b) for a, b in v)) for k, v in self.events.items()}
+
+
+PROFILE = None
+
+
+def _timed(kind, fn, *a):
+    return PROFILE.wrap(kind, fn, *a) if PROFILE is not None else fn(*a)
+
+
 class DugksRun(torch.autograd.Function):
     @staticmethod
     def forward(ctx, f0, eng, istep0, nsteps, every):
@@ -184,9 +213,9 @@ class DugksObjectiveRun(torch.autograd.Function):
 
         def advance(a, b):
             for k in range(a, b):
-                eng.step(istep0 + k)
+                _timed("forward step", eng.step, istep0 + k)
                 with torch.no_grad():
-                    J.add_(value(state).double())
+                    _timed("forward objective", lambda: J.add_(value(state).double()))
 
         k = 0
         for a in acts[:end]:
@@ -194,7 +223,7 @@ class DugksObjectiveRun(torch.autograd.Function):
                 advance(a[1], a[2])
                 k = a[2]
             else:
-                eng.get_state_device(stored.store(a[1]).data_ptr())
+                _timed("forward store", eng.get_state_device, stored.store(a[1]).data_ptr())
         advance(k, nsteps)
         out = empty_state(eng, f0.device)
         eng.get_state_device(out.data_ptr())
@@ -219,9 +248,15 @@ class DugksObjectiveRun(torch.autograd.Function):
             lam = lam_out.detach().contiguous().clone()
         dphi_direct = torch.zeros(phi.shape, dtype=torch.float64, device=phi.device)
         cur = engine_state(eng)  # the engine's current state (read by the adjoint and the sources)
+        # objectives with `prepare_adjoint(phi, w)` give a per-state source for the fixed control
+        # (a few kernels per step) and the direct phi-gradient summed over all steps at the end
+        fast = objective.prepare_adjoint(phi.detach(), w) if hasattr(objective, "prepare_adjoint") else None
 
         def source(state):
             nonlocal dphi_direct
+            if fast is not None:
+                _timed("adjoint source", fast[0], lam, state)
+                return
             acc = getattr(objective, "accumulate", None)
             if acc is not None:
                 dphi_direct += acc(lam, state, phi.detach(), w).double()
@@ -238,25 +273,28 @@ class DugksObjectiveRun(torch.autograd.Function):
 
         # source at the final state f_n
         eng.set_state_device(stored[ctx.last].data_ptr())
-        eng.run(istep0 + ctx.last, n - ctx.last) if n > ctx.last else None
+        if n > ctx.last:
+            _timed("recompute", eng.run, istep0 + ctx.last, n - ctx.last)
         source(cur)
         # resume the schedule from the last state of the forward sweep
         eng.set_state_device(stored[ctx.last].data_ptr())
         for a in ctx.acts[ctx.end:]:
             kind = a[0]
             if kind == "advance":
-                eng.run(istep0 + a[1], a[2] - a[1])
+                _timed("recompute", eng.run, istep0 + a[1], a[2] - a[1])
             elif kind == "store":
-                eng.get_state_device(stored.store(a[1]).data_ptr())
+                _timed("store", eng.get_state_device, stored.store(a[1]).data_ptr())
             elif kind == "restore":
-                eng.set_state_device(stored[a[1]].data_ptr())
+                _timed("restore", eng.set_state_device, stored[a[1]].data_ptr())
             elif kind == "release":
                 stored.release(a[1])
             else:  # adjoint of step k at the current state k (the engine's own buffer)
                 k = a[1]
-                eng.adjoint_step(istep0 + k, cur.data_ptr(), lam.data_ptr(), lam.data_ptr())
+                _timed("adjoint step", eng.adjoint_step, istep0 + k, cur.data_ptr(), lam.data_ptr(), lam.data_ptr())
                 if k >= 1:
                     source(cur)
+        if fast is not None:
+            dphi_direct += fast[1]()
         dphi = torch.from_numpy(eng.field_grad(reset=True)).to(phi.device) + dphi_direct
         ctx.stored = None
         return lam, dphi.to(phi.dtype), None, None, None, None, None, None
@@ -324,6 +362,34 @@ class WallShear:
             Fs = self.F + phi[:, :, ii].to(state.dtype)
             tot = tot + (self.nu / d) * (js + self.hdt * rho * Fs).sum()
         return tot / self.area
+
+    def prepare_adjoint(self, phi, w):
+        """(add, finish) for the reversal with phi and the weight w fixed: the
+        source this objective adds to the adjoint at every state is constant,
+        (w nu / (d area)) (c_s + hdt F_s) on the two wall planes, so it is formed
+        once and `add(lam, state)` adds it with one kernel; the direct phi
+        gradient, (w nu hdt / (d area)) rho at the wall cells of every state, is
+        summed per state into one FP64 buffer and `finish()` scales it once."""
+        nx = self.eng.nx
+        dev = phi.device
+        dt = state_dtype(self.eng)
+        idx = torch.tensor([0, nx - 1], device=dev)
+        cs = self.cs.to(torch.float64).to(dev).view(19, 1, 1, 1)
+        k = torch.stack([w * (self.nu / self.d0) / self.area, w * (self.nu / self.d1) / self.area]).to(dev)
+        Fs = (self.F + phi[:, :, [0, nx - 1]].double()).unsqueeze(0)            # (1, nz, ny, 2)
+        S = (k * (cs + self.hdt * Fs)).to(dt)                                   # (19, nz, ny, 2)
+        rho_sum = torch.zeros((self.eng.nz, self.eng.ny, 2), dtype=torch.float64, device=dev)
+
+        def add(lam, state):
+            soa_view(self.eng, lam).index_add_(3, idx, S)
+            rho_sum.add_(soa_view(self.eng, state).index_select(3, idx).sum(0, dtype=torch.float64))
+
+        def finish():
+            dphi = torch.zeros(phi.shape, dtype=torch.float64, device=dev)
+            dphi[:, :, [0, nx - 1]] = k * self.hdt * rho_sum
+            return dphi
+
+        return add, finish
 
     def accumulate(self, lam, state, phi, w):
         lo_l, hi_l = self._planes(lam)

@@ -71,6 +71,7 @@ static void FN(make_coef)(const oracle_cfg *c, FN(coef_t) *q)
     }
 }
 
+#ifndef ORACLE_TANGENT
 int FN(oracle_coefficients)(const oracle_cfg *c, double *out13)
 {
     FN(coef_t) q;
@@ -81,6 +82,7 @@ int FN(oracle_coefficients)(const oracle_cfg *c, double *out13)
     out13[9] = q.dx; out13[10] = q.dy; out13[11] = q.dz; out13[12] = q.dt;
     return 0;
 }
+#endif /* ORACLE_TANGENT */
 
 /* Equilibrium, src/dugks.cu:1201-1207 (feq_s) and 1183-1190 (inline in calc_fb1). */
 static inline REAL FN(feq_s)(REAL r, REAL u, REAL v, REAL w, REAL tp, int cx, int cy, int cz)
@@ -760,6 +762,7 @@ int FN(oracle_macro)(const oracle_cfg *c, const REAL *f, REAL *rho, REAL *ux, RE
     return 0;
 }
 
+#ifndef ORACLE_TANGENT
 /* diag.dat and profiles-2.dat statistics, src/output.cu:223-334
  * (statistics_serial), on global non-ghosted arrays ijk=(k*ny+j)*nx+i.
  * diag: mean rho,u,v,w; min rho,u,v,w; max rho,u,v,w.
@@ -837,3 +840,4 @@ int FN(oracle_stats)(int nx, int ny, int nz, const REAL *rhg, const REAL *uxg, c
     }
     return 0;
 }
+#endif /* ORACLE_TANGENT */

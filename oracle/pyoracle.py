@@ -164,6 +164,18 @@ class Oracle:
         assert rc == 0, rc
         return f
 
+    def tangent_run(self, f, df, istep0, nsteps, nthreads=0):
+        """Forward-mode tangent of nsteps steps (FP64): f <- S^n(f) and
+        df <- dS^n(f)[df] in place, both ghosted (liboracle's restatement run on
+        dual numbers, libtangent.so)."""
+        assert self.sfx == "f64"
+        for a in (f, df):
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.shape == self.shape
+        rc = tangent_lib().oracle_tangent_run(ctypes.byref(self.cfg), f.ctypes.data_as(_D), df.ctypes.data_as(_D),
+                                              istep0, nsteps, nthreads)
+        assert rc == 0, rc
+        return f, df
+
     def macro(self, f):
         out = [np.zeros(self.shape[:3], dtype=self.dtype) for _ in range(4)]
         getattr(lib(), f"oracle_macro_{self.sfx}")(ctypes.byref(self.cfg), self._p(f), *[self._p(a) for a in out])
@@ -275,6 +287,21 @@ def setup_from_config(text, dtype=np.float64, workdir="."):
     return dict(kv=kv, case=kv["case"], nx=nx, ny=ny, nz=nz, dx=float(dx), dy=float(dy), dz=float(dz),
                 dt=float(dt), visc=float(visc), F=F, xwidth=float(xw), ywidth=float(yw), zwidth=float(zw),
                 periodic_x=_stoi(kv["periods_x"]), perturb=_stoi(kv["perturb"]), xc=xc, dxx=dxx)
+
+
+_tan = None
+
+
+def tangent_lib():
+    global _tan
+    if _tan is None:
+        path = os.path.join(HERE, "libtangent.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        L.oracle_tangent_run.argtypes = [ctypes.POINTER(Cfg), _D, _D, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        _tan = L
+    return _tan
 
 
 def to_ghosted(f_dump, dtype=np.float64):

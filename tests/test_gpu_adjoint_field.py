@@ -145,15 +145,21 @@ def test_wall_shear_fast_source_equals_autograd_source():
     eng, f0d = _channel()
     obj = da.WallShear(eng, axis=2)
     plain = lambda s, p: obj(s, p)  # noqa: E731  (no `accumulate`: torch autograd path)
+
+    class PerStep:  # `accumulate` per state, without the prepared constant source
+        __call__ = staticmethod(obj.__call__)
+        accumulate = staticmethod(obj.accumulate)
+
     phi0 = torch.from_numpy(_field(eng, 10)).cuda()
     out = []
-    for o in (obj, plain):
+    for o in (obj, PerStep(), plain):
         phi = phi0.clone().requires_grad_(True)
         t0 = da.from_dump_order(eng, f0d).requires_grad_(True)
         _, j = da.run_objective(t0, phi, eng, 1, 9, o, snaps=4, axis=2)
         out.append(torch.autograd.grad(j, [phi, t0]))
-    for a, b in zip(out[0], out[1]):
-        assert float((a - b).abs().max()) <= 1e-12 * float(b.abs().max())
+    for got in out[:2]:
+        for a, b in zip(got, out[2]):
+            assert float((a - b).abs().max()) <= 1e-12 * float(b.abs().max())
 
 
 @pytest.mark.parametrize("case,axis", [("walls", 2), ("periodic", 0), ("stretched", 2), ("aniso", None)])
