@@ -684,6 +684,29 @@ int step_form(dg_ctx *h, int istep0, int n, cudaEvent_t *ev)
     return DG_OK;
 }
 
+// n steps from the state at src into the state at dst (device arrays in the
+// engine's SoA layout): the first step reads src and writes dst, the others
+// update dst in place.  The handle's own state is src or dst only when the
+// caller passes it.
+template <class T, class S>
+int step_between_form(dg_ctx *h, int istep0, int n, const void *src, void *dst)
+{
+    using K = Kern<T, S>;
+    const S *fi = static_cast<const S *>(src);
+    S *fo = static_cast<S *>(dst);
+    S *fb = static_cast<S *>(h->fb);
+    StepParams<T, S> P = params_for<T, S>(h, istep0);
+    for (int s = 0; s < n; ++s) {
+        if (h->perturb && s > 0) P = params_for<T, S>(h, istep0 + s);
+        set_round_seed<T, S>(h, P.codec, istep0 + s);
+        const S *in = s == 0 ? fi : fo;
+        CK(K::fbar(in, fb, P, h->stream), "stage (a) launch");
+        CK(K::flux(fb, in, fo, P, h->recon, h->have_tmap ? &h->tmap : nullptr, h->stream), "flux launch");
+    }
+    if (fo == h->f) h->macro_valid = false;
+    return DG_OK;
+}
+
 template <class T, class S>
 int set_state_form(dg_ctx *h, const double *host_dump)
 {
@@ -1397,6 +1420,23 @@ int dg_run(dg_t *h, int istep0, int nsteps)
     if (nsteps < 0) return h->fail(DG_ERR_ARG, "nsteps < 0");
     if (nsteps == 0) return DG_OK;
     return DISPATCH(h, step_form, istep0, nsteps, (cudaEvent_t *)nullptr);
+}
+
+int dg_run_between(dg_t *h, int istep0, int nsteps, const void *src, void *dst)
+{
+    if (!h) return DG_ERR_ARG;
+    if (nsteps < 0) return h->fail(DG_ERR_ARG, "nsteps < 0");
+    if (nsteps == 0) return DG_OK;
+    if (!src) src = h->f;
+    if (!dst) dst = h->f;
+    const size_t sb = size_t(h->ps) * 19 * storage_bytes(h->prec);
+    const char *lo = static_cast<const char *>(dst), *fb = static_cast<const char *>(h->fb);
+    if (lo < fb + size_t(h->ps_b) * 19 * storage_bytes(h->prec) && fb < lo + sb)
+        return h->fail(DG_ERR_ARG, "dg_run_between: the destination overlaps f-bar-plus");
+    const char *si = static_cast<const char *>(src);
+    if (si != lo && si < lo + sb && lo < si + sb)
+        return h->fail(DG_ERR_ARG, "dg_run_between: source and destination overlap without being equal");
+    return DISPATCH(h, step_between_form, istep0, nsteps, src, dst);
 }
 
 int dg_run_profiled(dg_t *h, int istep0, int nsteps, double *kernel_ms)

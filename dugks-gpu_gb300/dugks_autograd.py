@@ -271,28 +271,53 @@ class DugksObjectiveRun(torch.autograd.Function):
             if gp is not None:
                 dphi_direct += gp.double()
 
+        # The current state lives either in the engine's own buffer (`cur`) or in a
+        # stored slot: advances step out of place from a slot (dg_run_between), an
+        # advance followed by a store writes its last state straight into the new
+        # slot, and a restore only points at the slot -- no state copies.
+        where = [stored[ctx.last]]  # tensor holding the current state
+        own = cur.data_ptr()
+
+        def same(x, y):
+            return x is not None and y is not None and x.data_ptr() == y.data_ptr()
+
+        def advance_to(a, b, dst):
+            src = None if where[0].data_ptr() == own else where[0].data_ptr()
+            _timed("recompute", eng.run_between, istep0 + a, b - a, src, None if dst.data_ptr() == own else dst.data_ptr())
+            where[0] = dst
+
         # source at the final state f_n
-        eng.set_state_device(stored[ctx.last].data_ptr())
         if n > ctx.last:
-            _timed("recompute", eng.run, istep0 + ctx.last, n - ctx.last)
-        source(cur)
+            advance_to(ctx.last, n, cur)
+        source(where[0])
         # resume the schedule from the last state of the forward sweep
-        eng.set_state_device(stored[ctx.last].data_ptr())
-        for a in ctx.acts[ctx.end:]:
+        where[0] = stored[ctx.last]
+        acts = ctx.acts[ctx.end:]
+        for i, a in enumerate(acts):
             kind = a[0]
             if kind == "advance":
-                _timed("recompute", eng.run, istep0 + a[1], a[2] - a[1])
+                nxt = acts[i + 1] if i + 1 < len(acts) else None
+                if nxt is not None and nxt[0] == "store" and nxt[1] == a[2]:
+                    advance_to(a[1], a[2], stored.store(a[2]))
+                else:
+                    advance_to(a[1], a[2], cur)
             elif kind == "store":
-                _timed("store", eng.get_state_device, stored.store(a[1]).data_ptr())
+                slot = stored.store(a[1])
+                if not same(where[0], slot):  # a store not written by the advance before it
+                    _timed("store", slot.copy_, where[0])
+                    where[0] = slot
             elif kind == "restore":
-                _timed("restore", eng.set_state_device, stored[a[1]].data_ptr())
+                where[0] = stored[a[1]]
             elif kind == "release":
+                if same(where[0], stored[a[1]]):
+                    where[0] = None
                 stored.release(a[1])
-            else:  # adjoint of step k at the current state k (the engine's own buffer)
+            else:  # adjoint of step k at the current state k
                 k = a[1]
-                _timed("adjoint step", eng.adjoint_step, istep0 + k, cur.data_ptr(), lam.data_ptr(), lam.data_ptr())
+                st = where[0]
+                _timed("adjoint step", eng.adjoint_step, istep0 + k, st.data_ptr(), lam.data_ptr(), lam.data_ptr())
                 if k >= 1:
-                    source(cur)
+                    source(st)
         if fast is not None:
             dphi_direct += fast[1]()
         dphi = torch.from_numpy(eng.field_grad(reset=True)).to(phi.device) + dphi_direct

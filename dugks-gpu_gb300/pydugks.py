@@ -80,6 +80,7 @@ def lib():
         "dg_step": (ctypes.c_int, [H, ctypes.c_int]),
         "dg_run": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_int]),
         "dg_run_profiled": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_int, _D]),
+        "dg_run_between": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]),
         "dg_sync": (ctypes.c_int, [H]),
         "dg_selftest_wait_timeout": (ctypes.c_int, [H, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
         "dg_upload_macro": (ctypes.c_int, [H]),
@@ -178,6 +179,11 @@ class Engine:
 
     def run(self, istep0, nsteps):
         self._check(lib().dg_run(self._h, istep0, nsteps))
+
+    def run_between(self, istep0, nsteps, src_ptr=None, dst_ptr=None):
+        """nsteps steps from the device state at src_ptr into dst_ptr (None: the engine's own state)."""
+        self._check(lib().dg_run_between(self._h, istep0, nsteps, None if src_ptr is None else ctypes.c_void_p(src_ptr),
+                                         None if dst_ptr is None else ctypes.c_void_p(dst_ptr)))
 
     def run_profiled(self, istep0, nsteps):
         """Run with per-kernel CUDA events; returns (ms of stage (a), ms of flux) summed over the steps."""

@@ -101,6 +101,17 @@ int dg_step(dg_t *h, int istep);
 /* Steps istep0 .. istep0+nsteps-1 back to back, asynchronous. */
 int dg_run(dg_t *h, int istep0, int nsteps);
 
+/* Steps istep0 .. istep0+nsteps-1 from the state at src into the state at
+ * dst, asynchronous (no counterpart in the reference; for checkpointed
+ * reversals, which step from a stored state without copying it in first):
+ * src and dst are device arrays in the engine's SoA state layout
+ * (19*pop_stride values of the storage type, like dg_device_ptr(h,
+ * DG_BUF_F)), NULL meaning the handle's own state.  The first step reads src
+ * and writes dst, the others update dst in place; src stays unchanged unless
+ * it equals dst, and the handle's own state changes only when it is dst.
+ * DG_ERR_ARG when dst overlaps f-bar-plus or src and dst overlap partly. */
+int dg_run_between(dg_t *h, int istep0, int nsteps, const void *src, void *dst);
+
 /* dg_run with every launch bracketed by CUDA events on the handle's stream;
  * waits for completion and returns the summed milliseconds of the stage (a)
  * launches in kernel_ms[0] and of the flux launches in kernel_ms[1]. */

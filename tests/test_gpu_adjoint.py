@@ -137,3 +137,33 @@ def test_gradient_of_kinetic_energy_matches_finite_differences():
         rel = abs(ad - float(fd)) / abs(float(fd))
         print(f"direction {k}: adjoint {ad:.10e} fd {float(fd):.10e} rel {rel:.2e}")
         assert rel < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32", "fp16"])
+def test_run_between_equals_the_in_place_run(precision):
+    """dg_run_between (steps from one device state into another, the handle's own
+    state untouched unless named) against dg_run in place: identical states."""
+    eng = _engine("stretched", precision)
+    eng.set_stream(torch.cuda.current_stream().cuda_stream)
+    eng.set_state(seeded_state(eng.nx, eng.ny, eng.nz, seed=24))
+    dt = {"fp64": torch.float64, "fp32": torch.float32, "fp16": torch.float16}[precision]
+    src = torch.empty(eng.soa_len, dtype=dt, device="cuda")
+    eng.get_state_device(src.data_ptr())
+    keep = src.clone()
+    dst = torch.full_like(src, float("nan"))
+    eng.run_between(5, 4, src.data_ptr(), dst.data_ptr())
+    own = torch.empty_like(src)
+    eng.get_state_device(own.data_ptr())
+    torch.cuda.synchronize()
+    assert torch.equal(src, keep) and torch.equal(own, keep)   # neither the source nor the handle's state moved
+    eng.run(5, 4)
+    eng.get_state_device(own.data_ptr())
+    torch.cuda.synchronize()
+    assert torch.equal(dst, own)
+    eng.run_between(9, 3, dst.data_ptr(), None)                   # into the handle's own state
+    eng.run_between(9, 3, dst.data_ptr(), dst.data_ptr())         # in place in dst
+    eng.get_state_device(own.data_ptr())
+    torch.cuda.synchronize()
+    assert torch.equal(dst, own)
+    with pytest.raises(pydugks.DugksError):
+        eng.run_between(1, 1, src.data_ptr(), eng.device_ptr(pydugks.DG_BUF_FB))
