@@ -19,7 +19,9 @@ FP64 are the sampling floor of a chaotic flow, the difference that any change
 of rounding makes to finite-time averages once the trajectories have
 decorrelated; errors of the reduced forms at that level are not precision
 errors.  `bf16n` is the BF16 form with round-to-nearest storage, `fp16s` the
-FP16 form with stochastic rounding.
+FP16 form with stochastic rounding.  With --start every form starts from the
+given state (a developed turbulent state from channel_spinup.py) instead of
+the seeded laminar start.
 
 Reference orientation: x wall-normal, y spanwise, z streamwise.
 
@@ -45,6 +47,8 @@ def run_form(form, args):
     cfg, meta = pydugks.channel_config(nx=args.nx, ny=args.ny, nz=args.nz, precision=prec, **extra)
     eng = pydugks.Engine(cfg)
     eng.set_stream(torch.cuda.current_stream().cuda_stream)
+    if args.start:
+        eng.set_state(np.load(args.start, mmap_mode="r"))
     if form == "fp64p":
         f = eng.get_state()
         r = np.random.default_rng(args.seed).uniform(-1.0, 1.0, f.shape)
@@ -97,6 +101,8 @@ def main():
     ap.add_argument("--forms", default="fp64,fp32,fp16,bf16")
     ap.add_argument("--pert", type=float, default=1e-12, help="relative perturbation of the fp64p start")
     ap.add_argument("--seed", type=int, default=1, help="seed of the fp64p perturbation")
+    ap.add_argument("--start", default="", help="start every form from this state (dump order, float64 .npy, "
+                    "e.g. a turbulent state from channel_spinup.py) instead of the seeded start")
     ap.add_argument("--save", default="", help="write the time-averaged profiles of every form to this .npz")
     ap.add_argument("--ref", default="", help="take the FP64 (and fp64p) results from a --save file of the "
                     "same workload instead of running them")
@@ -117,6 +123,7 @@ def main():
             res[p] = run_form(p, args)
     ref = res["fp64"]
     out = {"workload": f"channel Re_tau=180 {args.nz}x{args.nx}x{args.ny} (stream x wall x span), tanh mesh",
+           "start": args.start or "seeded perturbed laminar start",
            "steps": args.steps, "burn": args.burn, "every": args.every, "samples": ref["count"],
            "wall_s": time.time() - t0, "forms": {}}
     if "fp64p" in forms:
