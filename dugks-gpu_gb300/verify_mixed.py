@@ -18,8 +18,9 @@ The form `fp64p` is FP64 from the same start with every value multiplied by
 FP64 are the sampling floor of a chaotic flow, the difference that any change
 of rounding makes to finite-time averages once the trajectories have
 decorrelated; errors of the reduced forms at that level are not precision
-errors.  `bf16n` is the BF16 form with round-to-nearest storage, `fp16s` the
-FP16 form with stochastic rounding.  With --start every form starts from the
+errors.  `bf16n` and `fp16n` are the 16-bit forms with round-to-nearest
+storage (the default is stochastic rounding), `fp16s` the FP16 form with
+stochastic rounding named explicitly.  With --start every form starts from the
 given state (a developed turbulent state from channel_spinup.py) instead of
 the seeded laminar start.
 
@@ -42,8 +43,9 @@ import pydugks  # noqa: E402
 
 def run_form(form, args):
     import torch
-    prec = {"fp64p": "fp64", "bf16n": "bf16", "fp16s": "fp16"}.get(form, form)
-    extra = {"bf16n": {"rounding": "nearest"}, "fp16s": {"rounding": "stochastic"}}.get(form, {})
+    prec = {"fp64p": "fp64", "bf16n": "bf16", "fp16n": "fp16", "fp16s": "fp16"}.get(form, form)
+    extra = {"bf16n": {"rounding": "nearest"}, "fp16n": {"rounding": "nearest"},
+             "fp16s": {"rounding": "stochastic"}}.get(form, {})
     cfg, meta = pydugks.channel_config(nx=args.nx, ny=args.ny, nz=args.nz, precision=prec, **extra)
     eng = pydugks.Engine(cfg)
     eng.set_stream(torch.cuda.current_stream().cuda_stream)

@@ -151,6 +151,7 @@ def test_run_between_equals_the_in_place_run(precision):
     eng.get_state_device(src.data_ptr())
     keep = src.clone()
     dst = torch.full_like(src, float("nan"))
+    cells = lambda t: da.to_dump_order(eng, t)  # noqa: E731  (the x pitch padding is never written)
     eng.run_between(5, 4, src.data_ptr(), dst.data_ptr())
     own = torch.empty_like(src)
     eng.get_state_device(own.data_ptr())
@@ -159,11 +160,11 @@ def test_run_between_equals_the_in_place_run(precision):
     eng.run(5, 4)
     eng.get_state_device(own.data_ptr())
     torch.cuda.synchronize()
-    assert torch.equal(dst, own)
+    assert torch.equal(cells(dst), cells(own))
     eng.run_between(9, 3, dst.data_ptr(), None)                   # into the handle's own state
     eng.run_between(9, 3, dst.data_ptr(), dst.data_ptr())         # in place in dst
     eng.get_state_device(own.data_ptr())
     torch.cuda.synchronize()
-    assert torch.equal(dst, own)
+    assert torch.equal(cells(dst), cells(own))
     with pytest.raises(pydugks.DugksError):
         eng.run_between(1, 1, src.data_ptr(), eng.device_ptr(pydugks.DG_BUF_FB))
