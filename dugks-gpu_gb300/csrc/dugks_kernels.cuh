@@ -46,6 +46,14 @@ constexpr int CW_Y8 = 56;    // + 8 (class-1) + q   y face, c_x, c_z != 0 (c_y =
 constexpr int CW_Z4 = 72;    // + 4 slot4z(p) + q   z face, c_x != 0 = c_y (p = 1, 2, 11..14)
 constexpr int CW_Z8 = 96;    // + 8 (class-1) + q   z face, c_x, c_y != 0 (c_z = 0)
 constexpr int CW_ROWS = 112;
+
+// Rows of the stretched-mesh gradient table P.gw (recon=gradient, mesh != uniform)
+constexpr int GW_LAM = 0;     // x face I: interpolation weight of cell I+1 at the face
+constexpr int GW_IDX = 1;     // x face I: 1 / (xc_{I+1} - xc_I)
+constexpr int GW_WM = 2;      // column i: three-point x derivative weights on xc_{i-1}, xc_i, xc_{i+1}
+constexpr int GW_W0 = 3;
+constexpr int GW_WP = 4;
+constexpr int GW_ROWS = 5;
 __host__ __device__ constexpr int slot4y(int p) { return p == 1 ? 0 : (p == 2 ? 1 : p - 5); }
 __host__ __device__ constexpr int slot4z(int p) { return p == 1 ? 0 : (p == 2 ? 1 : p - 9); }
 
@@ -94,6 +102,8 @@ struct StepParams {
     const T *xw;                 // [19*2][xws] x-face normal (1-m, m) of face I (between cells I, I+1, 1-based)
     const T *txw;                // [19*2][xws] transverse x (1-t, t) per column 0..nx+1
     int xws;                     // row stride of xw / txw (nx+2)
+    const T *gw;                 // [GW_ROWS][xws] gradient reconstruction weights of a stretched x mesh
+    int grad_st;                 // 1: recon=gradient on a stretched x mesh (face_grad reads gw)
     const T *cxu;                // [nx+2] dt/dxx(i)
     const T *cxuf;               // [nx+2] fw1*dt/dxx(i)
     // perturbation forcing (src/dugks.cu:1086-1126) as separable factors
@@ -1016,17 +1026,34 @@ __device__ __forceinline__ void face_grad(const StepParams<T, S> &P, const RD &R
             const int L = i, Rr = i + 1;  // left / right column of face I = i
             const RI r = R.rb(jc, kc);
             const T a = R(p, r, Rr), b = R(p, r, L);
-            temp = T(0.5) * (a + b);
-            gx = (a - b) * P.g_idx;
             const RI ru = R.rb(jp, kc), rd = R.rb(jm, kc);
-            gy = (T(0.5) * (R(p, ru, L) + R(p, ru, Rr)) - T(0.5) * (R(p, rd, L) + R(p, rd, Rr))) * P.g_i2dy;
             const RI rt = R.rb(jc, kp), rbo = R.rb(jc, km);
-            gz = (T(0.5) * (R(p, rt, L) + R(p, rt, Rr)) - T(0.5) * (R(p, rbo, L) + R(p, rbo, Rr))) * P.g_i2dz;
+            if (P.grad_st) {
+                // stretched x mesh: values interpolated to the face, normal difference over the centre spacing
+                const T lam = __ldg(P.gw + GW_LAM * P.xws + i), idx = __ldg(P.gw + GW_IDX * P.xws + i);
+                temp = fma(lam, a - b, b);
+                gx = (a - b) * idx;
+                const T bu = R(p, ru, L), bd = R(p, rd, L), bt = R(p, rt, L), bb = R(p, rbo, L);
+                gy = (fma(lam, R(p, ru, Rr) - bu, bu) - fma(lam, R(p, rd, Rr) - bd, bd)) * P.g_i2dy;
+                gz = (fma(lam, R(p, rt, Rr) - bt, bt) - fma(lam, R(p, rbo, Rr) - bb, bb)) * P.g_i2dz;
+            } else {
+                temp = T(0.5) * (a + b);
+                gx = (a - b) * P.g_idx;
+                gy = (T(0.5) * (R(p, ru, L) + R(p, ru, Rr)) - T(0.5) * (R(p, rd, L) + R(p, rd, Rr))) * P.g_i2dy;
+                gz = (T(0.5) * (R(p, rt, L) + R(p, rt, Rr)) - T(0.5) * (R(p, rbo, L) + R(p, rbo, Rr))) * P.g_i2dz;
+            }
         } else if (AX == 1) {
             const RI rD = R.rb(jc, kc), rU = R.rb(jp, kc);
             const T a = R(p, rU, i), b = R(p, rD, i);
             temp = T(0.5) * (a + b);
-            gx = (T(0.5) * (R(p, rD, i + 1) + R(p, rU, i + 1)) - T(0.5) * (R(p, rD, i - 1) + R(p, rU, i - 1))) * P.g_i2dx;
+            if (P.grad_st) {
+                // three-point x derivative of the face averages on the non-uniform centres
+                gx = __ldg(P.gw + GW_WM * P.xws + i) * (T(0.5) * (R(p, rD, i - 1) + R(p, rU, i - 1)));
+                gx = fma(__ldg(P.gw + GW_W0 * P.xws + i), temp, gx);
+                gx = fma(__ldg(P.gw + GW_WP * P.xws + i), T(0.5) * (R(p, rD, i + 1) + R(p, rU, i + 1)), gx);
+            } else {
+                gx = (T(0.5) * (R(p, rD, i + 1) + R(p, rU, i + 1)) - T(0.5) * (R(p, rD, i - 1) + R(p, rU, i - 1))) * P.g_i2dx;
+            }
             gy = (a - b) * P.g_idy;
             const RI tD = R.rb(jc, kp), tU = R.rb(jp, kp), bD = R.rb(jc, km), bU = R.rb(jp, km);
             gz = (T(0.5) * (R(p, tD, i) + R(p, tU, i)) - T(0.5) * (R(p, bD, i) + R(p, bU, i))) * P.g_i2dz;
@@ -1034,7 +1061,13 @@ __device__ __forceinline__ void face_grad(const StepParams<T, S> &P, const RD &R
             const RI rB = R.rb(jc, kc), rT = R.rb(jc, kp);
             const T a = R(p, rT, i), b = R(p, rB, i);
             temp = T(0.5) * (a + b);
-            gx = (T(0.5) * (R(p, rB, i + 1) + R(p, rT, i + 1)) - T(0.5) * (R(p, rB, i - 1) + R(p, rT, i - 1))) * P.g_i2dx;
+            if (P.grad_st) {
+                gx = __ldg(P.gw + GW_WM * P.xws + i) * (T(0.5) * (R(p, rB, i - 1) + R(p, rT, i - 1)));
+                gx = fma(__ldg(P.gw + GW_W0 * P.xws + i), temp, gx);
+                gx = fma(__ldg(P.gw + GW_WP * P.xws + i), T(0.5) * (R(p, rB, i + 1) + R(p, rT, i + 1)), gx);
+            } else {
+                gx = (T(0.5) * (R(p, rB, i + 1) + R(p, rT, i + 1)) - T(0.5) * (R(p, rB, i - 1) + R(p, rT, i - 1))) * P.g_i2dx;
+            }
             const RI uB = R.rb(jp, kc), uT = R.rb(jp, kp), dB = R.rb(jm, kc), dT = R.rb(jm, kp);
             gy = (T(0.5) * (R(p, uB, i) + R(p, uT, i)) - T(0.5) * (R(p, dB, i) + R(p, dT, i))) * P.g_i2dy;
             gz = (a - b) * P.g_idz;

@@ -133,8 +133,8 @@ struct dg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     void *f = nullptr, *fb = nullptr;
-    void *tab = nullptr;          // xw | txw | cxu | pert_x | pert_y | pert_z | cxuf | cw (T-typed)
-    size_t tab_off[8] = {};
+    void *tab = nullptr;          // xw | txw | cxu | pert_x | pert_y | pert_z | cxuf | cw | gw (T-typed)
+    size_t tab_off[9] = {};
     double *macro = nullptr;      // rho|ux|uy|uz ghosted
     double *scratch = nullptr;    // statistics partial sums / moments partials
     size_t scratch_bytes = 0;
@@ -267,7 +267,6 @@ int load_config(dg_ctx *h, const ConfigFile &cf)
     if (!(h->cfl > 0) || !(h->xwidth > 0) || !(h->ywidth > 0) || !(h->zwidth > 0))
         return h->fail(DG_ERR_CONFIG, "CFL and the widths must be > 0");
     if (h->mesh != 0 && h->periodic[0]) return h->fail(DG_ERR_CONFIG, "a stretched mesh needs walls in x (periods_x=0)");
-    if (h->recon == 1 && h->mesh != 0) return h->fail(DG_ERR_UNSUPPORTED, "recon=gradient needs a uniform mesh");
     return DG_OK;
 }
 
@@ -333,7 +332,8 @@ struct YZWeights {
 // dt/dxx, perturbation factors)
 template <class T, class R>
 void make_tables(const dg_ctx *h, const RefCoef<R> &c, std::vector<T> &xw, std::vector<T> &txw, std::vector<T> &cxu,
-                 std::vector<T> &px, std::vector<T> &py, std::vector<T> &pz, std::vector<T> &cxuf, std::vector<T> &cw)
+                 std::vector<T> &px, std::vector<T> &py, std::vector<T> &pz, std::vector<T> &cxuf, std::vector<T> &cw,
+                 std::vector<T> &gw)
 {
     const int nx = h->nx, ny = h->ny, nz = h->nz;
     const bool st = h->mesh != 0;
@@ -374,6 +374,31 @@ void make_tables(const dg_ctx *h, const RefCoef<R> &c, std::vector<T> &xw, std::
                 txw[size_t(2 * p) * xs + gi] = T(R(1 - t));
                 txw[size_t(2 * p + 1) * xs + gi] = T(t);
             }
+        }
+    }
+    // gradient reconstruction on a stretched x mesh (recon=gradient, mesh !=
+    // uniform), rows of GW_* per column, computed in double from the mesh:
+    //   x face I (between cells I and I+1): the face value is the linear
+    //   interpolation of the two cell values to the face, weight lam_I =
+    //   (dxx_I/2) / (xc_{I+1} - xc_I) on cell I+1, and the normal derivative is
+    //   their difference over xc_{I+1} - xc_I;
+    //   y and z faces at column i: the x derivative of the face-averaged values
+    //   is the three-point central difference on the non-uniform centres
+    //   xc_{i-1}, xc_i, xc_{i+1} (exact for quadratics).
+    // On a uniform mesh these are 1/2, 1/dx and (-1/(2dx), 0, 1/(2dx)): the
+    // reference's calc_fx (src/dugks.cu:421-649).
+    gw.assign(xs * dg::GW_ROWS, T(0));
+    if (st) {
+        for (int I = 0; I <= nx; ++I) {
+            const double d = h->xc[I + 1] - h->xc[I];
+            gw[size_t(dg::GW_LAM) * xs + I] = T(0.5 * h->dxx[I] / d);
+            gw[size_t(dg::GW_IDX) * xs + I] = T(1.0 / d);
+        }
+        for (int i = 1; i <= nx; ++i) {
+            const double hm = h->xc[i] - h->xc[i - 1], hp = h->xc[i + 1] - h->xc[i];
+            gw[size_t(dg::GW_WM) * xs + i] = T(-hp / (hm * (hp + hm)));
+            gw[size_t(dg::GW_W0) * xs + i] = T((hp - hm) / (hp * hm));
+            gw[size_t(dg::GW_WP) * xs + i] = T(hm / (hp * (hp + hm)));
         }
     }
     // corner weights: products of the lerp weights as T values, evaluated in
@@ -541,6 +566,8 @@ StepParams<T, S> make_params(const dg_ctx *h, const RefCoef<R> &c)
     P.cxu = reinterpret_cast<const T *>(base + h->tab_off[2]);
     P.cxuf = reinterpret_cast<const T *>(base + h->tab_off[6]);
     P.cw = reinterpret_cast<const T *>(base + h->tab_off[7]);
+    P.gw = reinterpret_cast<const T *>(base + h->tab_off[8]);
+    P.grad_st = (h->recon == 1 && h->mesh != 0) ? 1 : 0;
     P.err = h->dev_err;
     P.pert_x = reinterpret_cast<const T *>(base + h->tab_off[3]);
     P.pert_y = reinterpret_cast<const T *>(base + h->tab_off[4]);
@@ -839,6 +866,7 @@ int adjoint_form(dg_ctx *h, int istep, const void *f_n, const void *lam_next, vo
 {
     using K = Kern<T, S>;
     if (!std::is_same<T, S>::value) return h->fail(DG_ERR_UNSUPPORTED, "the adjoint exists for the fp64 and fp32 forms");
+    if (h->recon != 0) return h->fail(DG_ERR_UNSUPPORTED, "the adjoint exists for the trilinear reconstruction");
     if (!h->adj) {
         // 19 adjoint values and one dJ/dF (force-field face term) per face, the
         // wall-ghost sums (2 * 19 per row and plane) and the transposed-stencil
@@ -1048,19 +1076,19 @@ int spectral_form(dg_ctx *h, double *vals, std::vector<double> *shells)
 template <class T>
 int upload_tables(dg_ctx *h)
 {
-    std::vector<T> xw, txw, cxu, px, py, pz, cxuf, cw;
+    std::vector<T> xw, txw, cxu, px, py, pz, cxuf, cw, gw;
     if (h->prec == DG_PREC_FP64)
-        make_tables<T, double>(h, h->c64, xw, txw, cxu, px, py, pz, cxuf, cw);
+        make_tables<T, double>(h, h->c64, xw, txw, cxu, px, py, pz, cxuf, cw, gw);
     else
-        make_tables<T, float>(h, h->c32, xw, txw, cxu, px, py, pz, cxuf, cw);
-    const std::vector<T> *parts[8] = {&xw, &txw, &cxu, &px, &py, &pz, &cxuf, &cw};
+        make_tables<T, float>(h, h->c32, xw, txw, cxu, px, py, pz, cxuf, cw, gw);
+    const std::vector<T> *parts[9] = {&xw, &txw, &cxu, &px, &py, &pz, &cxuf, &cw, &gw};
     size_t off = 0;
-    for (int t = 0; t < 8; ++t) {
+    for (int t = 0; t < 9; ++t) {
         h->tab_off[t] = off;
         off += (parts[t]->size() * sizeof(T) + 255) / 256 * 256;
     }
     CK(cudaMalloc(&h->tab, off), "cudaMalloc (tables)");
-    for (int t = 0; t < 8; ++t)
+    for (int t = 0; t < 9; ++t)
         CK(cudaMemcpy(static_cast<char *>(h->tab) + h->tab_off[t], parts[t]->data(), parts[t]->size() * sizeof(T),
                       cudaMemcpyHostToDevice),
            "table upload");

@@ -574,6 +574,70 @@ static void FN(cell_tri)(const oracle_cfg *c, const FN(coef_t) *q, REAL *f, cons
 #undef FBV
 }
 
+/* The gradient reconstruction on a stretched x mesh (no counterpart in the
+ * reference, whose stretched-mesh channel reconstructs trilinearly; this is
+ * calc_fx's rule on non-uniform centres): an x face between cells a and a+1
+ * takes the cell values interpolated linearly to the face, weight
+ * lam = (dxx_a/2)/(xc_{a+1} - xc_a) on cell a+1, and the normal derivative
+ * (f_{a+1} - f_a)/(xc_{a+1} - xc_a); the x derivative on y and z faces is the
+ * three-point central difference of the face-averaged values on the centres
+ * xc_{i-1}, xc_i, xc_{i+1}.  On a uniform mesh both reduce to calc_fx. */
+static void FN(cell_grad_stretched)(const oracle_cfg *c, const FN(coef_t) *q, REAL *f, const REAL *fb, int i, int j,
+                                    int k)
+{
+    const int nx = c->nx, ny = c->ny;
+    const REAL hdt = q->hdt, dy = q->dy, dz = q->dz;
+    const double *xc = c->xc, *dxx = c->dxx;
+    REAL ft[6][19];
+    int ip, s;
+    const double hm = xc[i] - xc[i - 1], hp = xc[i + 1] - xc[i];
+    const REAL wm = (REAL)(-hp / (hm * (hp + hm))), w0 = (REAL)((hp - hm) / (hp * hm)), wp = (REAL)(hm / (hp * (hp + hm)));
+#define FBV(ip_, a_, b_, c_) fb[IDX(ip_, a_, b_, c_)]
+    for (s = 0; s < 2; s++) {               /* x faces: s = 1 between i and i+1, s = 0 between i-1 and i */
+        const int a = s == 1 ? i : i - 1, b = a + 1;
+        const REAL lam = (REAL)(0.5 * dxx[a] / (xc[b] - xc[a])), id = (REAL)(1.0 / (xc[b] - xc[a]));
+        for (ip = 0; ip < 19; ip++) {
+            REAL temp = FBV(ip, a, j, k) + lam * (FBV(ip, b, j, k) - FBV(ip, a, j, k));
+            REAL gradx = (FBV(ip, b, j, k) - FBV(ip, a, j, k)) * id;
+            REAL aa = FBV(ip, a, j + 1, k) + lam * (FBV(ip, b, j + 1, k) - FBV(ip, a, j + 1, k));
+            REAL bb = FBV(ip, a, j - 1, k) + lam * (FBV(ip, b, j - 1, k) - FBV(ip, a, j - 1, k));
+            REAL grady = (aa - bb) / (2 * dy);
+            aa = FBV(ip, a, j, k + 1) + lam * (FBV(ip, b, j, k + 1) - FBV(ip, a, j, k + 1));
+            bb = FBV(ip, a, j, k - 1) + lam * (FBV(ip, b, j, k - 1) - FBV(ip, a, j, k - 1));
+            REAL gradz = (aa - bb) / (2 * dz);
+            ft[s][ip] = ip == 0 ? temp : temp - hdt * (CIX[ip] * gradx + CIY[ip] * grady + CIZ[ip] * gradz);
+        }
+    }
+    FN(bounce_back)(c, i, ft);
+    for (s = 2; s < 6; s++) {               /* y faces (2: j-1|j, 3: j|j+1), z faces (4: k-1|k, 5: k|k+1) */
+        const int y = s < 4, up = s & 1;
+        const int j0 = y ? (up ? j : j - 1) : j, k0 = y ? k : (up ? k : k - 1);
+        const int j1 = y ? j0 + 1 : j0, k1 = y ? k0 : k0 + 1;
+        for (ip = 0; ip < 19; ip++) {
+            REAL temp = 0.5 * (FBV(ip, i, j1, k1) + FBV(ip, i, j0, k0));
+            REAL gradx = wm * (0.5 * (FBV(ip, i - 1, j0, k0) + FBV(ip, i - 1, j1, k1))) + w0 * temp +
+                         wp * (0.5 * (FBV(ip, i + 1, j0, k0) + FBV(ip, i + 1, j1, k1)));
+            REAL gn = y ? (FBV(ip, i, j1, k1) - FBV(ip, i, j0, k0)) / dy : (FBV(ip, i, j1, k1) - FBV(ip, i, j0, k0)) / dz;
+            REAL gt;   /* transverse: z on a y face, y on a z face, central over 2 cells */
+            if (y) {
+                REAL aa = 0.5 * (FBV(ip, i, j0, k + 1) + FBV(ip, i, j1, k + 1));
+                REAL bb = 0.5 * (FBV(ip, i, j0, k - 1) + FBV(ip, i, j1, k - 1));
+                gt = (aa - bb) / (2 * dz);
+            } else {
+                REAL aa = 0.5 * (FBV(ip, i, j + 1, k0) + FBV(ip, i, j + 1, k1));
+                REAL bb = 0.5 * (FBV(ip, i, j - 1, k0) + FBV(ip, i, j - 1, k1));
+                gt = (aa - bb) / (2 * dy);
+            }
+            {
+                const REAL grady = y ? gn : gt, gradz = y ? gt : gn;
+                ft[s][ip] = temp - hdt * (CIX[ip] * gradx + CIY[ip] * grady + CIZ[ip] * gradz);
+            }
+        }
+    }
+    FN(face_fluxes_and_update)(c, q, f, fb, i, j, k, ft);
+#undef FBV
+}
+
 /* Stages (b)(c) with the central-difference ("gradient") reconstruction,
  * src/dugks.cu:421-584 (calc_fx), followed by the shared (d)(e). */
 static void FN(cell_grad)(const oracle_cfg *c, const FN(coef_t) *q, REAL *f, const REAL *fb, int i, int j, int k)
@@ -583,6 +647,10 @@ static void FN(cell_grad)(const oracle_cfg *c, const FN(coef_t) *q, REAL *f, con
     REAL ft[6][19];
     int ip;
     REAL temp, aa, bb, gradx, grady, gradz;
+    if (c->mesh == 1) {
+        FN(cell_grad_stretched)(c, q, f, fb, i, j, k);
+        return;
+    }
 #define FBV(ip_, a_, b_, c_) fb[IDX(ip_, a_, b_, c_)]
     for (ip = 0; ip < 19; ip++) {
         temp = 0.5 * (FBV(ip, i + 1, j, k) + FBV(ip, i, j, k));
@@ -676,7 +744,6 @@ static int FN(check_cfg)(const oracle_cfg *c)
 {
     if (c->nx < 3 || c->ny < 1 || c->nz < 1) return -1;
     if (c->mesh == 1 && (c->xc == 0 || c->dxx == 0)) return -2;
-    if (c->recon == 1 && c->mesh == 1) return -3;
     return 0;
 }
 

@@ -38,9 +38,10 @@ def test_fp32_matches_oracle(case):
     assert err <= FP32_TOL
 
 
-@pytest.mark.parametrize("case", ["walls", "periodic", "aniso"])
+@pytest.mark.parametrize("case", ["walls", "periodic", "aniso", "stretched"])
 def test_gradient_reconstruction_matches_oracle(case):
-    """recon=gradient: the central-difference variant of src/dugks.cu:421-649 (calc_fx)."""
+    """recon=gradient: the central-difference variant of src/dugks.cu:421-649 (calc_fx); on the
+    tanh-stretched mesh with the face-interpolated values and non-uniform central differences."""
     from _cases import CASES as C
     import pydugks
     import pyoracle
@@ -58,7 +59,7 @@ def test_gradient_reconstruction_matches_oracle(case):
     assert err <= FP64_TOL
 
 
-@pytest.mark.parametrize("case", ["walls", "periodic"])
+@pytest.mark.parametrize("case", ["walls", "periodic", "stretched"])
 def test_gradient_reconstruction_fp32_matches_oracle(case):
     """recon=gradient in the FP32 form (the TMA-staged flux kernel) against the FP32 oracle."""
     from _cases import CASES as C
@@ -180,3 +181,18 @@ def test_graph_replayed_run_equals_single_steps(prec):
     for s in range(38, 59):
         b.step(s)
     assert np.array_equal(a.get_state(), b.get_state())
+
+
+def test_adjoint_refuses_the_gradient_reconstruction():
+    """The hand-written adjoint transposes the trilinear reconstruction only."""
+    import ctypes
+    import pydugks
+    from _cases import CASES as C
+    kw = dict(C["walls"])
+    kw["recon"] = "gradient"
+    import torch
+    eng = pydugks.Engine(pydugks.make_config(**kw))
+    lam = torch.zeros(2, eng.soa_len, dtype=torch.float64, device="cuda")
+    rc = pydugks.lib().dg_adjoint_step(eng._h, 1, ctypes.c_void_p(eng.device_ptr(pydugks.DG_BUF_F)),
+                                       ctypes.c_void_p(lam[0].data_ptr()), ctypes.c_void_p(lam[1].data_ptr()))
+    assert rc == pydugks.DG_ERR_UNSUPPORTED

@@ -155,3 +155,25 @@ def test_oracle_matches_reference_golden(path):
     err = rel_err(pyoracle.interior(f), m["f_out"])
     tol = 1e-13 if dtype == np.float64 else 2e-6
     assert err <= tol, err
+
+
+def test_stretched_gradient_reconstruction_reduces_to_the_uniform_one(tmp_path):
+    """recon=gradient on a stretched mesh whose faces are evenly spaced (a mesh
+    file) equals the reference's uniform calc_fx rule to rounding."""
+    import pydugks
+    from seeded import seeded_state
+    kw = dict(nx=12, ny=5, nz=4, xwidth=12, ywidth=5, zwidth=4, periods_x=0, CFL=0.5, visc=0.02, ambient_fz=1e-5,
+              recon="gradient")
+    with open(tmp_path / "mesh.txt", "w") as fh:
+        fh.write("\n".join(repr(float(v)) for v in np.arange(13.0)) + "\n")
+    uni = pyoracle.Oracle.from_config(pydugks.make_config(**kw))
+    st = pyoracle.Oracle.from_config(pydugks.make_config(mesh="file", mesh_file="mesh.txt", **kw),
+                                     workdir=str(tmp_path))
+    assert st.cfg.mesh == 1 and st.cfg.recon == 1 and uni.cfg.mesh == 0
+    f0 = pyoracle.to_ghosted(seeded_state(12, 5, 4, seed=41))
+    a, b = f0.copy(), f0.copy()
+    uni.run(a, 1, 10)
+    st.run(b, 1, 10)
+    err = float(np.max(np.abs(a - b)) / np.max(np.abs(a)))
+    print(f"stretched rule on a uniform mesh vs calc_fx: {err:.2e}")
+    assert err <= 1e-13

@@ -26,7 +26,8 @@ def _setup(case, recon=0):
     return orc, f, d
 
 
-@pytest.mark.parametrize("case,recon", [(c, 0) for c in sorted(CASES)] + [("walls", 1), ("periodic", 1)])
+@pytest.mark.parametrize("case,recon", [(c, 0) for c in sorted(CASES)] + [("walls", 1), ("periodic", 1),
+                                                                          ("stretched", 1)])
 def test_tangent_is_the_derivative_of_the_oracle_step(case, recon):
     orc, f, d = _setup(case, recon)
     fv, dv = f.copy(), d.copy()
