@@ -734,17 +734,31 @@ int step_between_form(dg_ctx *h, int istep0, int n, const void *src, void *dst)
     return DG_OK;
 }
 
+// Device staging of a dump-order double array (host transfers of the state):
+// f-bar-plus when it is large enough (the FP64 form: every step rewrites it,
+// so between steps it is free), else a temporary allocation (*owned = true).
+double *state_staging(dg_ctx *h, size_t bytes, bool *owned)
+{
+    *owned = false;
+    if (h->fb && size_t(h->ps_b) * 19 * storage_bytes(h->prec) >= bytes) return static_cast<double *>(h->fb);
+    double *tmp = nullptr;
+    if (cudaMalloc(&tmp, bytes) != cudaSuccess) return nullptr;
+    *owned = true;
+    return tmp;
+}
+
 template <class T, class S>
 int set_state_form(dg_ctx *h, const double *host_dump)
 {
     using K = Kern<T, S>;
     const size_t n = h->ncell() * 19;
-    double *tmp = nullptr;
-    CK(cudaMalloc(&tmp, n * sizeof(double)), "cudaMalloc (state upload)");
+    bool owned = false;
+    double *tmp = state_staging(h, n * sizeof(double), &owned);
+    if (!tmp) return h->fail(DG_ERR_CUDA, "cudaMalloc (state upload staging) failed");
     cudaError_t e = cudaMemcpyAsync(tmp, host_dump, n * sizeof(double), cudaMemcpyHostToDevice, h->stream);
     if (e == cudaSuccess) e = K::aos_to_soa(tmp, static_cast<S *>(h->f), params_for<T, S>(h, 0), h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    cudaFree(tmp);
+    if (owned) cudaFree(tmp);
     if (e != cudaSuccess) return h->cuda_fail(e, "state upload");
     h->macro_valid = false;
     return DG_OK;
@@ -755,12 +769,13 @@ int get_state_form(dg_ctx *h, double *host_dump)
 {
     using K = Kern<T, S>;
     const size_t n = h->ncell() * 19;
-    double *tmp = nullptr;
-    CK(cudaMalloc(&tmp, n * sizeof(double)), "cudaMalloc (state download)");
+    bool owned = false;
+    double *tmp = state_staging(h, n * sizeof(double), &owned);
+    if (!tmp) return h->fail(DG_ERR_CUDA, "cudaMalloc (state download staging) failed");
     cudaError_t e = K::soa_to_aos(static_cast<const S *>(h->f), tmp, params_for<T, S>(h, 0), h->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(host_dump, tmp, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
-    cudaFree(tmp);
+    if (owned) cudaFree(tmp);
     if (e != cudaSuccess) return h->cuda_fail(e, "state download");
     return DG_OK;
 }
