@@ -78,6 +78,23 @@ __global__ void __launch_bounds__(1024) stats_partials_kernel(const S *__restric
     for (int s = 0; s < NSTAT; ++s) out[s] = acc[s];
 }
 
+// Ordered reduction over blocks of the statistics partials of x index i:
+// acc[s] = sum / min / max over b of partial[b][i][s] (b ascending).  Shared by
+// stats_reduce_kernel and the allocation-free statistics, so that both give
+// the same numbers.
+__device__ __forceinline__ void stats_combine_blocks(const double *__restrict__ partial, int nblocks, int nx, int i,
+                                                     double acc[NSTAT])
+{
+    for (int s = 0; s < NSTAT; ++s) acc[s] = partial[size_t(i) * NSTAT + s];
+    for (int b = 1; b < nblocks; ++b) {
+        const double *q = partial + (size_t(b) * nx + i) * NSTAT;
+        for (int s = 0; s < 10; ++s) acc[s] += q[s];
+        for (int s = 10; s < 14; ++s) acc[s] = fmin(acc[s], q[s]);
+        for (int s = 14; s < 18; ++s) acc[s] = fmax(acc[s], q[s]);
+        acc[18] += q[18];
+    }
+}
+
 // Ordered reduction over blocks: total[i][s] = sum/min/max over b of partial[b][i][s].
 __global__ void stats_reduce_kernel(const double *__restrict__ partial, int nblocks, int nx, double *__restrict__ total);
 // acc[i][s] += total[i][s] for the 10 sums

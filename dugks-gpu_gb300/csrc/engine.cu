@@ -1325,14 +1325,7 @@ __global__ void stats_reduce_kernel(const double *__restrict__ partial, int nblo
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nx) return;
     double acc[NSTAT];
-    for (int s = 0; s < NSTAT; ++s) acc[s] = partial[size_t(i) * NSTAT + s];
-    for (int b = 1; b < nblocks; ++b) {
-        const double *q = partial + (size_t(b) * nx + i) * NSTAT;
-        for (int s = 0; s < 10; ++s) acc[s] += q[s];
-        for (int s = 10; s < 14; ++s) acc[s] = fmin(acc[s], q[s]);
-        for (int s = 14; s < 18; ++s) acc[s] = fmax(acc[s], q[s]);
-        acc[18] += q[18];
-    }
+    stats_combine_blocks(partial, nblocks, nx, i, acc);
     for (int s = 0; s < NSTAT; ++s) total[size_t(i) * NSTAT + s] = acc[s];
 }
 

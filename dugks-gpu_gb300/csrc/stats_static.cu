@@ -74,14 +74,7 @@ __global__ void noalloc_reduce_kernel(const double *__restrict__ partial, int nb
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nx) return;
     double acc[dg::NSTAT];
-    for (int s = 0; s < dg::NSTAT; ++s) acc[s] = partial[size_t(i) * dg::NSTAT + s];
-    for (int b = 1; b < nblocks; ++b) {
-        const double *q = partial + (size_t(b) * nx + i) * dg::NSTAT;
-        for (int s = 0; s < 10; ++s) acc[s] += q[s];
-        for (int s = 10; s < 14; ++s) acc[s] = fmin(acc[s], q[s]);
-        for (int s = 14; s < 18; ++s) acc[s] = fmax(acc[s], q[s]);
-        acc[18] += q[18];
-    }
+    dg::stats_combine_blocks(partial, nblocks, nx, i, acc);  // the reduction of dg_stats_values
     for (int s = 0; s < dg::NSTAT; ++s) total[size_t(i) * dg::NSTAT + s] = acc[s];
     const double n = double(nyz);
     const double ua = acc[1] / n, va = acc[2] / n, wa = acc[3] / n;
