@@ -1208,8 +1208,8 @@ __device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const RD 
     T v[NPOP];
     if constexpr (RECON == 0 && Fp64Form<T>::value)
         face_tri_cw<T, S, AX>(P, R, i, j, k, v);
-    else if constexpr (RECON == 0 && std::is_same<S, float>::value)
-        face_tri_x2<S, AX>(P, R, i, j, k, v);  // FP32 form (the 16-bit forms measured slower packed)
+    else if constexpr (RECON == 0 && (std::is_same<S, float>::value || std::is_same<S, __nv_bfloat16>::value))
+        face_tri_x2<S, AX>(P, R, i, j, k, v);  // packed lerps: FP32 and BF16 (FP16 measured 3 % slower packed)
     else if constexpr (RECON == 0)
         face_tri<T, S, AX>(P, R, i, j, k, v);
     else
