@@ -117,3 +117,18 @@ def test_host_driver_matches_the_abi_loop(tmp_path):
     assert a == b
     assert (tmp_path / "drv" / "diag.dat").read_text() == (tmp_path / "abi" / "diag.dat").read_text()
     assert len((tmp_path / "drv" / "diag.dat").read_text().splitlines()) == 3  # steps 1, 3, 6
+
+
+def test_host_driver_writes_the_profiles_fixture_the_reference_script_read(tmp_path):
+    """The host driver on tests/golden/laminar_profiles_config.txt writes profiles-2.dat
+    byte for byte as tests/golden/laminar_profiles-2.dat, the file that the reference's
+    own ProcessProfiles.py was run on (tests/test_postprocessing.py)."""
+    if not os.path.exists(DRIVER):
+        pytest.skip("host driver not built")
+    golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    with open(os.path.join(golden, "laminar_profiles_config.txt")) as fh:
+        (tmp_path / "config.txt").write_text(fh.read())
+    r = subprocess.run([DRIVER, "config.txt", "--quiet"], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    with open(os.path.join(golden, "laminar_profiles-2.dat"), "rb") as fh:
+        assert (tmp_path / "profiles-2.dat").read_bytes() == fh.read()
