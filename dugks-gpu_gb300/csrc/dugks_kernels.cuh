@@ -508,10 +508,10 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
 // for the interior columns and rows.
 // ---------------------------------------------------------------------------
 template <class T, class S>
-__global__ void __launch_bounds__(256) fb_ghost_kernel(S *__restrict__ fb, const StepParams<T, S> P)
+__global__ void __launch_bounds__(256) fb_ghost_kernel(S *__restrict__ fb, const StepParams<T, S> P, int skip_x)
 {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
-    const long long nxg = 2LL * (ny + 2) * (nz + 2);
+    const long long nxg = skip_x ? 0 : 2LL * (ny + 2) * (nz + 2);
     const long long nyg = 2LL * nx * (nz + 2);
     const long long nzg = 2LL * nx * ny;
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1425,6 +1425,35 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
         phase ^= 1u << s;
     };
 
+    // 16-bit forms between walls: the wall ghost columns 0 and nx+1 of f-bar-plus
+    // are not stored (fb_ghost_kernel skips them); the tiles that read them form
+    // them in shared memory from the landed plane, g0 = q0 d(1) + (1-q0) d(2),
+    // g_{nx+1} = q1 d(nx) + (1-q1) d(nx-1) (src/dugks.cu:1234-1251; stretched
+    // mesh src/fortran/channel/src/dugks.cuf:365-374), on the stored deviations
+    // (the decode is affine) and rounded to the nearest 16-bit value.  Column 0
+    // is read only by the first tile, column nx+1 only by the tile holding nx.
+    // (Formed by the whole CTA after each plane lands, with one more block
+    // barrier in those tiles; done by the halo warp one plane ahead instead, it
+    // measured slower.)
+    constexpr bool WALL_GHOST = sizeof(S) == 2;
+    const int cwall_lo = (WALL_GHOST && !P.periodic_x && i0 == 1) ? 0 : -1;
+    const int cwall_hi = (WALL_GHOST && !P.periodic_x && i0 <= nx && nx <= i0 + 31) ? nx + 1 - (i0 - 1) : -1;
+    auto wall_ghosts = [&](int g) {
+        if constexpr (WALL_GHOST) {
+            S *st = reinterpret_cast<S *>(smem) + (g & 3) * RD::STAGE;
+            for (int t = tid; t < 2 * NPOP * RD::RH; t += 32 * W) {
+                const int side = t / (NPOP * RD::RH), seg = t - side * (NPOP * RD::RH);
+                const int c = side ? cwall_hi : cwall_lo;
+                if (c < 0) continue;
+                S *row = st + seg * RD::BXT;  // segment = one row of one population
+                const int d = side ? -1 : 1;
+                const float q = side ? float(P.q1) : float(P.q0);
+                const float a = float(row[c + d]), b = float(row[c + 2 * d]);
+                row[c] = S(q * a + (1.0f - q) * b);
+            }
+        }
+    };
+
     const int gi = i0 + lane;
     const int gj = j0 + wr - 1;
     const bool cell = wr >= 1 && gi <= nx && gj <= ny;
@@ -1438,9 +1467,19 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
     int buf = 0;
     wait(kb - 1);
     wait(kb);
+    const bool wall_tile = cwall_lo >= 0 || cwall_hi >= 0;  // the same for the whole CTA
+    if (wall_tile) {
+        wall_ghosts(kb - 1);
+        wall_ghosts(kb);
+        __syncthreads();
+    }
     if (wr >= 1) face_fluxes<T, S, 2, RECON, FF>(P, R, ci, cj, kb - 1, fzd);
     for (int k = kb; k < ke; ++k) {
         wait(k + 1);
+        if (wall_tile) {
+            wall_ghosts(k + 1);
+            __syncthreads();
+        }
         if (wr >= 1) {
             face_fluxes<T, S, 0, RECON, FF>(P, R, ci, cj, k, fx);
             face_fluxes<T, S, 1, RECON, FF>(P, R, ci, cj, k, fy);

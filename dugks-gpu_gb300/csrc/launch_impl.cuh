@@ -23,8 +23,11 @@ cudaError_t Kern<T, S>::fbar(const S *f, S *fb, const StepParams<T, S> &P, cudaS
         const int bx = P.nx >= 128 ? 128 : ((P.nx + 31) / 32) * 32;
         dim3 grid((P.nx + bx - 1) / bx, P.ny, P.nz);
         fbar_kernel<T, S, false><<<grid, bx, 0, st>>>(f, fb, P, 0);
-        const long long ghosts = 2LL * (P.ny + 2) * (P.nz + 2) + 2LL * P.nx * (P.nz + 2) + 2LL * P.nx * P.ny;
-        fb_ghost_kernel<T, S><<<unsigned((ghosts + 255) / 256), 256, 0, st>>>(fb, P);
+        // the 16-bit forms' flux kernel forms the wall ghost columns itself (in shared memory)
+        const int skip_x = (sizeof(S) == 2 && !P.periodic_x) ? 1 : 0;
+        const long long ghosts = (skip_x ? 0 : 2LL * (P.ny + 2) * (P.nz + 2)) + 2LL * P.nx * (P.nz + 2) +
+                                 2LL * P.nx * P.ny;
+        fb_ghost_kernel<T, S><<<unsigned((ghosts + 255) / 256), 256, 0, st>>>(fb, P, skip_x);
     }
     return cudaGetLastError();
 }

@@ -46,7 +46,8 @@ typedef struct dg_ctx dg_t;
 #define DG_BUF_F 0              /* f-tilde, structure of arrays */
 #define DG_BUF_FB 1             /* f-bar-plus, structure of arrays with x ghost columns 0, nx+1; scratch
                                  * of every step and of the host state transfers (dg_set_state,
-                                 * dg_get_state, dg_copy_ddf, dg_dump), which may overwrite it */
+                                 * dg_get_state, dg_copy_ddf, dg_dump), which may overwrite it; the
+                                 * fp16 / bf16 forms between walls do not store its x ghost columns */
 #define DG_BUF_RHO 2            /* ghosted scalar macro arrays (after dg_upload_macro) */
 #define DG_BUF_UX 3
 #define DG_BUF_UY 4
