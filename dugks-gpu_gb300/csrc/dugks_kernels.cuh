@@ -277,8 +277,10 @@ __device__ __forceinline__ void copy_images(S *fb, long long ps_b, int I, int J,
     }
 }
 
-// Stage (a) for one cell.  GHOST = false: the interior of f-bar-plus only
-// (fb_ghost_kernel fills the ghost layer).  GHOST = true: the ghost layer is
+// Stage (a) for one cell.  GHOST = 0: the interior of f-bar-plus only
+// (fb_ghost_kernel fills the ghost layer).  GHOST = 2: the interior and its
+// periodic images in y and z only (the 16-bit forms between walls, whose flux
+// kernel forms the wall ghost columns itself).  GHOST = 1: the ghost layer is
 // written by the threads that hold its sources, in the same launch -- a cell
 // of the first/last row or plane also writes its periodic images in y and z
 // (src/dugks.cu:1256-1273, src/parallel.cu:192-199), the first/last cell of a
@@ -331,7 +333,7 @@ __device__ __forceinline__ void fbar_one_axis(T r, T u, T vv, T w, T B, T Kb, T 
     pair(16, 17, w3 - v3, 2);
 }
 
-template <class T, class S, bool GHOST>
+template <class T, class S, int GHOST>
 __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *__restrict__ fb, const StepParams<T, S> P,
                                                    int xoff)
 {
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     const bool in = i >= 0 && i < nx;
     const int wbase = blockIdx.x * blockDim.x + (threadIdx.x & ~31) - xoff;  // cell of lane 0
     const bool wall_warp =
-        GHOST && !P.periodic_x && ((wbase <= 1 && wbase + 31 >= 0) || (wbase <= nx - 1 && wbase + 31 >= nx - 2));
+        GHOST == 1 && !P.periodic_x && ((wbase <= 1 && wbase + 31 >= 0) || (wbase <= nx - 1 && wbase + 31 >= nx - 2));
     if (!in && !wall_warp) return;
     const int ic = in ? i : (i < 0 ? 0 : nx - 1);  // lanes past the row read a valid cell and store nothing
     const long long c = ((long long)k * ny + j) * P.pitch + ic;
@@ -439,7 +441,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     const bool small = ny == 1 || nz == 1;  // two images along one axis: copied at the end
     const bool img = !small && (dj != 0 || dk != 0);
     const bool xend = wbase <= 0 || wbase + 31 >= nx - 1;
-    if (!GHOST || (!wall_warp && !img && !small && !(P.periodic_x && xend))) {
+    if (GHOST == 0 || (!wall_warp && !img && !small && !(P.periodic_x && xend))) {
 #pragma unroll
         for (int p = 0; p < NPOP; ++p) fb[p * P.ps_b + cb] = P.codec.encode_h(p, ob[p], hc);
         return;
@@ -490,8 +492,9 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     }
     if (small && in) {
         copy_images(fb, P.ps_b, ic + 1, j + 1, k + 1, ny, nz, P.pitch_b);
-        if (ic == 0) copy_images(fb, P.ps_b, P.periodic_x ? nx + 1 : 0, j + 1, k + 1, ny, nz, P.pitch_b);
-        if (ic == nx - 1) copy_images(fb, P.ps_b, P.periodic_x ? 0 : nx + 1, j + 1, k + 1, ny, nz, P.pitch_b);
+        if (GHOST == 1 && ic == 0) copy_images(fb, P.ps_b, P.periodic_x ? nx + 1 : 0, j + 1, k + 1, ny, nz, P.pitch_b);
+        if (GHOST == 1 && ic == nx - 1)
+            copy_images(fb, P.ps_b, P.periodic_x ? 0 : nx + 1, j + 1, k + 1, ny, nz, P.pitch_b);
     }
 }
 
@@ -508,10 +511,10 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
 // for the interior columns and rows.
 // ---------------------------------------------------------------------------
 template <class T, class S>
-__global__ void __launch_bounds__(256) fb_ghost_kernel(S *__restrict__ fb, const StepParams<T, S> P, int skip_x)
+__global__ void __launch_bounds__(256) fb_ghost_kernel(S *__restrict__ fb, const StepParams<T, S> P)
 {
     const int nx = P.nx, ny = P.ny, nz = P.nz;
-    const long long nxg = skip_x ? 0 : 2LL * (ny + 2) * (nz + 2);
+    const long long nxg = 2LL * (ny + 2) * (nz + 2);
     const long long nyg = 2LL * nx * (nz + 2);
     const long long nzg = 2LL * nx * ny;
     long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1426,7 +1429,8 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
     };
 
     // 16-bit forms between walls: the wall ghost columns 0 and nx+1 of f-bar-plus
-    // are not stored (fb_ghost_kernel skips them); the tiles that read them form
+    // are not stored (stage (a) writes the interior and its y / z images only);
+    // the tiles that read them form
     // them in shared memory from the landed plane, g0 = q0 d(1) + (1-q0) d(2),
     // g_{nx+1} = q1 d(nx) + (1-q1) d(nx-1) (src/dugks.cu:1234-1251; stretched
     // mesh src/fortran/channel/src/dugks.cuf:365-374), on the stored deviations

@@ -16,18 +16,21 @@ cudaError_t Kern<T, S>::fbar(const S *f, S *fb, const StepParams<T, S> &P, cudaS
         const int xoff = (!P.periodic_x && P.nx % 32 == 1) ? 1 : 0;
         const int bx = P.nx + xoff >= 128 ? 128 : ((P.nx + xoff + 31) / 32) * 32;
         dim3 grid((P.nx + xoff + bx - 1) / bx, P.ny, P.nz);
-        fbar_kernel<T, S, true><<<grid, bx, 0, st>>>(f, fb, P, xoff);
+        fbar_kernel<T, S, 1><<<grid, bx, 0, st>>>(f, fb, P, xoff);
     } else {
-        // FP64 and 16-bit storage: the fused ghost writes cost more issue in stage (a)
-        // (FP64 pipe, 16-bit encode) than the separate pass saves
         const int bx = P.nx >= 128 ? 128 : ((P.nx + 31) / 32) * 32;
         dim3 grid((P.nx + bx - 1) / bx, P.ny, P.nz);
-        fbar_kernel<T, S, false><<<grid, bx, 0, st>>>(f, fb, P, 0);
-        // the 16-bit forms' flux kernel forms the wall ghost columns itself (in shared memory)
-        const int skip_x = (sizeof(S) == 2 && !P.periodic_x) ? 1 : 0;
-        const long long ghosts = (skip_x ? 0 : 2LL * (P.ny + 2) * (P.nz + 2)) + 2LL * P.nx * (P.nz + 2) +
-                                 2LL * P.nx * P.ny;
-        fb_ghost_kernel<T, S><<<unsigned((ghosts + 255) / 256), 256, 0, st>>>(fb, P, skip_x);
+        if (sizeof(S) == 2 && !P.periodic_x) {
+            // 16-bit storage between walls: stage (a) also writes the y / z images (the same
+            // encoded values); the flux kernel forms the wall ghost columns in shared memory
+            fbar_kernel<T, S, 2><<<grid, bx, 0, st>>>(f, fb, P, 0);
+        } else {
+            // FP64 and periodic 16-bit storage: the fused ghost writes cost more issue in
+            // stage (a) (FP64 pipe, 16-bit encode) than the separate pass saves
+            fbar_kernel<T, S, 0><<<grid, bx, 0, st>>>(f, fb, P, 0);
+            const long long ghosts = 2LL * (P.ny + 2) * (P.nz + 2) + 2LL * P.nx * (P.nz + 2) + 2LL * P.nx * P.ny;
+            fb_ghost_kernel<T, S><<<unsigned((ghosts + 255) / 256), 256, 0, st>>>(fb, P);
+        }
     }
     return cudaGetLastError();
 }
