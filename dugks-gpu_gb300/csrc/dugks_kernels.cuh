@@ -187,6 +187,36 @@ __device__ __forceinline__ T upd_base(T fb, T fo, T c43, T c13)
     return sizeof(T) == 8 ? fma(fb, c43, -(fo * c13)) : fma(fb - fo, c13, fb);
 }
 
+// New f-tilde of one population of a cell: the first term (upd_base of its
+// f-bar-plus and f-tilde as stored) plus coef x (flux difference) along each
+// axis it moves on (src/dugks.cu:949-956), then the stored value.  Plain
+// forms: the terms are added to the first term in axis order.  16-bit forms:
+// the first term is in deviation units (an affine combination of stored
+// deviations, coefficients summing to one) and the flux terms in f units with
+// the rest state cancelled, so they are summed apart and scaled once,
+// d = base + sum / s_p, then rounded as every stored deviation.
+template <class T, class S>
+struct UpdateSum {
+    T r, acc = T(0);
+    int nt = 0;
+    __device__ __forceinline__ explicit UpdateSum(T base) : r(base) {}
+    __device__ __forceinline__ void add(T coef, T diff)
+    {
+        if constexpr (Codec<T, S>::deviation)
+            acc = nt ? fma(coef, diff, acc) : coef * diff;
+        else
+            r = fma(coef, diff, r);
+        ++nt;
+    }
+    __device__ __forceinline__ S encode(const Codec<T, S> &c, int p, unsigned hc) const
+    {
+        if constexpr (Codec<T, S>::deviation)
+            return c.encode_dh(p, nt ? fma(c.is[p], acc, r) : r, hc);
+        else
+            return c.encode_h(p, r, hc);
+    }
+};
+
 // All 19 equilibria for density r and velocity (u, v, w).
 template <class T>
 __device__ __forceinline__ void feq_all(T r, T u, T v, T w, T fe[NPOP])
@@ -591,6 +621,7 @@ struct FbRead {
     }
     __device__ __forceinline__ T raw(int p, long long row, int col) const { return codec.raw_nc(fb, p * ps + row + col); }
     __device__ __forceinline__ T dec(int p, T x) const { return codec.dec(p, x); }
+    __device__ __forceinline__ T dec_e(int p, T x) const { return codec.dec_e(p, x); }
 };
 
 // 19 reconstructed values of one face, trilinear characteristic interpolation
@@ -603,10 +634,11 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
 {
     using RI = decltype(R.rb(0, 0));
     // j, k are stored indices (ghost rows / planes 0 and n+1 hold the periodic images).
-    // The stencil is read undecoded (R.raw) and each face value decoded once
-    // (R.dec): the interpolation is affine with weights summing to one, so for
-    // the 16-bit deviation forms s (sum w d) + w_eq equals sum w (s d + w_eq);
-    // for FP64 / FP32 both are the identity and the arithmetic is unchanged.
+    // The stencil is read undecoded (R.raw) and each face value scaled once
+    // (R.dec_e): the interpolation is affine with weights summing to one, so for
+    // the 16-bit deviation forms s (sum w d) is the face value less its rest
+    // state w_p (the form the face flux takes); for FP64 / FP32 both are the
+    // identity and the arithmetic is unchanged.
     const int jm = j - 1, jp = j + 1, jc = j;
     const int km = k - 1, kp = k + 1, kc = k;
     if (AX == 0) {
@@ -615,7 +647,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
         // representative population (1: cx>0, 2: cx<0, 3: cx=0), one load per class
         const T *xw = P.xw + i;
         const RI r00 = R.rb(jc, kc);
-        v[0] = R.dec(0, T(0.5) * (R.raw(0, r00, A) + R.raw(0, r00, B)));
+        v[0] = R.dec_e(0, T(0.5) * (R.raw(0, r00, A) + R.raw(0, r00, B)));
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ay = cy(p), az = cz(p);
@@ -637,15 +669,15 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
                     const RI r11 = R.rb(jt, kt);
                     y11 = lerp2(P.ty_om, P.ty_m, x10, lerp2(om, m, R.raw(p, r11, A), R.raw(p, r11, B)));
                 }
-                v[p] = R.dec(p, lerp2(P.tz_om, P.tz_m, y00, y11));
+                v[p] = R.dec_e(p, lerp2(P.tz_om, P.tz_m, y00, y11));
             } else {
-                v[p] = R.dec(p, y00);
+                v[p] = R.dec_e(p, y00);
             }
         }
     } else if (AX == 1) {
         // rows j (anchor) and j+1 (other); transverse x to column i - cx, z to plane k - cz
         const RI rA = R.rb(jc, kc), rB = R.rb(jp, kc);
-        v[0] = R.dec(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+        v[0] = R.dec_e(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
         const T *tw = P.txw + i;
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
@@ -667,15 +699,15 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
                     x10 = lerp2(txo, txm, x10, R.raw(p, sA, io));
                     x11 = lerp2(txo, txm, x11, R.raw(p, sB, io));
                 }
-                v[p] = R.dec(p, lerp2(P.tz_om, P.tz_m, y00, lerp2(P.yn_om[p], P.yn_m[p], x10, x11)));
+                v[p] = R.dec_e(p, lerp2(P.tz_om, P.tz_m, y00, lerp2(P.yn_om[p], P.yn_m[p], x10, x11)));
             } else {
-                v[p] = R.dec(p, y00);
+                v[p] = R.dec_e(p, y00);
             }
         }
     } else {
         // planes k (anchor) and k+1 (other); transverse x to i - cx, y to row j - cy
         const RI rA = R.rb(jc, kc), rB = R.rb(jc, kp);
-        v[0] = R.dec(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+        v[0] = R.dec_e(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
         const T *tw = P.txw + i;
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
@@ -700,7 +732,7 @@ __device__ __forceinline__ void face_tri(const StepParams<T, S> &P, const RD &R,
                 y00 = lerp2(P.ty_om, P.ty_m, x00, x01);
                 y11 = lerp2(P.ty_om, P.ty_m, x10, x11);
             }
-            v[p] = R.dec(p, lerp2(P.zn_om[p], P.zn_m[p], y00, y11));
+            v[p] = R.dec_e(p, lerp2(P.zn_om[p], P.zn_m[p], y00, y11));
         }
     }
 }
@@ -767,7 +799,7 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
         const float om3 = __ldg(xw + 6 * xs), m3 = __ldg(xw + 7 * xs);
         const float2 om33 = make_float2(om3, om3), m33 = make_float2(m3, m3);
         const RI r00 = R.rb(jc, kc);
-        v[0] = R.dec(0, 0.5f * (R.raw(0, r00, A) + R.raw(0, r00, B)));
+        v[0] = R.dec_e(0, 0.5f * (R.raw(0, r00, A) + R.raw(0, r00, B)));
 #pragma unroll
         for (int n = 0; n < 9; ++n) {
             const int p = pair_p(0, n), q = pair_q(0, n);
@@ -798,13 +830,13 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
                 }
                 res = lerp_x2(tz_o, tz_m, y00, y11);
             }
-            v[p] = R.dec(p, res.x);
-            v[q] = R.dec(q, res.y);
+            v[p] = R.dec_e(p, res.x);
+            v[q] = R.dec_e(q, res.y);
         }
     } else if (AX == 1) {
         // rows j (A) and j+1 (B); transverse x to column i - cx, z to plane k - cz
         const RI rA = R.rb(jc, kc), rB = R.rb(jp, kc);
-        v[0] = R.dec(0, 0.5f * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+        v[0] = R.dec_e(0, 0.5f * (R.raw(0, rA, i) + R.raw(0, rB, i)));
         const float *tw = P.txw + i;
         const float2 tx_o = make_float2(__ldg(tw + 2 * xs), __ldg(tw + 4 * xs));
         const float2 tx_m = make_float2(__ldg(tw + 3 * xs), __ldg(tw + 5 * xs));
@@ -833,13 +865,13 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
                 }
                 res = lerp_x2(tz_o, tz_m, y00, lerp_x2(yo, ym, x10, x11));
             }
-            v[p] = R.dec(p, res.x);
-            v[q] = R.dec(q, res.y);
+            v[p] = R.dec_e(p, res.x);
+            v[q] = R.dec_e(q, res.y);
         }
     } else {
         // planes k (A) and k+1 (B); transverse x to column i - cx, y to row j - cy
         const RI rA = R.rb(jc, kc), rB = R.rb(jc, kp);
-        v[0] = R.dec(0, 0.5f * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+        v[0] = R.dec_e(0, 0.5f * (R.raw(0, rA, i) + R.raw(0, rB, i)));
         const float *tw = P.txw + i;
         const float2 tx_o = make_float2(__ldg(tw + 2 * xs), __ldg(tw + 4 * xs));
         const float2 tx_m = make_float2(__ldg(tw + 3 * xs), __ldg(tw + 5 * xs));
@@ -869,8 +901,8 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
                 y11 = lerp_x2(ty_o, ty_m, x10, x11);
             }
             const float2 res = lerp_x2(zo, zm, y00, y11);
-            v[p] = R.dec(p, res.x);
-            v[q] = R.dec(q, res.y);
+            v[p] = R.dec_e(p, res.x);
+            v[q] = R.dec_e(q, res.y);
         }
     }
 }
@@ -895,7 +927,7 @@ __device__ __forceinline__ void face_tri_cw(const StepParams<T, S> &P, const RD 
         const int A = i == 0 ? 1 : i, B = i == 0 ? 0 : i + 1;
         const T *xw = P.xw + i;
         const RI r00 = R.rb(jc, kc);
-        v[0] = R.dec(0, T(0.5) * (R.raw(0, r00, A) + R.raw(0, r00, B)));
+        v[0] = R.dec_e(0, T(0.5) * (R.raw(0, r00, A) + R.raw(0, r00, B)));
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ay = cy(p), az = cz(p), c = xrep(p);
@@ -930,12 +962,12 @@ __device__ __forceinline__ void face_tri_cw(const StepParams<T, S> &P, const RD 
                 t = fma(__ldg(w + 6 * xs), R.raw(p, r11, A), t);
                 t = fma(__ldg(w + 7 * xs), R.raw(p, r11, B), t);
             }
-            v[p] = R.dec(p, t);
+            v[p] = R.dec_e(p, t);
         }
     } else if (AX == 1) {
         // rows j (A) and j+1 (B); transverse x to column i - cx, z to plane k - cz
         const RI rA = R.rb(jc, kc), rB = R.rb(jp, kc);
-        v[0] = R.dec(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+        v[0] = R.dec_e(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ax = cx(p), az = cz(p), c = xrep(p);
@@ -968,12 +1000,12 @@ __device__ __forceinline__ void face_tri_cw(const StepParams<T, S> &P, const RD 
                 t = fma(__ldg(w + 6 * xs), R.raw(p, sB, i), t);
                 t = fma(__ldg(w + 7 * xs), R.raw(p, sB, io), t);
             }
-            v[p] = R.dec(p, t);
+            v[p] = R.dec_e(p, t);
         }
     } else {
         // planes k (A) and k+1 (B); transverse x to column i - cx, y to row j - cy
         const RI rA = R.rb(jc, kc), rB = R.rb(jc, kp);
-        v[0] = R.dec(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
+        v[0] = R.dec_e(0, T(0.5) * (R.raw(0, rA, i) + R.raw(0, rB, i)));
 #pragma unroll
         for (int p = 1; p < NPOP; ++p) {
             const int ax = cx(p), ay = cy(p), c = xrep(p);
@@ -1006,7 +1038,7 @@ __device__ __forceinline__ void face_tri_cw(const StepParams<T, S> &P, const RD 
                 t = fma(__ldg(w + 6 * xs), R.raw(p, sB, i), t);
                 t = fma(__ldg(w + 7 * xs), R.raw(p, sB, io), t);
             }
-            v[p] = R.dec(p, t);
+            v[p] = R.dec_e(p, t);
         }
     }
 }
@@ -1093,6 +1125,10 @@ __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[N
 {
     T r, jx, jy, jz;
     moments(v, r, jx, jy, jz);
+    // 16-bit forms: v holds f_p - w_p; the rest state adds sum w_p = 1 to the
+    // density and nothing to the momentum, and out carries F_p - w_p, which the
+    // update only differences between the two faces of a cell
+    if constexpr (Codec<T, S>::deviation) r += T(1);
     const T inv = recip(r);
     T u = jx * inv, vv = jy * inv, w = jz * inv;
     T B = P.fw2s;
@@ -1217,6 +1253,11 @@ __device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const RD 
         face_tri<T, S, AX>(P, R, i, j, k, v);
     else
         face_grad<T, S, AX>(P, R, i, j, k, v);
+    if constexpr (RECON != 0 && Codec<T, S>::deviation) {
+        // the face values less their rest state, as the interpolating forms give them
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) v[p] -= P.codec.w[p];
+    }
     if (AX == 0 && !P.periodic_x) bounce_back(v, i == 0, i == P.nx);
     face_flux<T, S, AX, FF>(P, v, out, FF ? face_field<T, S, AX>(P, i, j, k) : T(0));
 }
@@ -1289,21 +1330,20 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_kernel(const S *__restrict_
                 const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
 #pragma unroll
                 for (int p = 0; p < NPOP; ++p) {
-                    const T fo = P.codec.load(f_in, p * P.ps + c, p);
-                    T r = upd_base(R(p, cb, 0), fo, c43, c13);
+                    UpdateSum<T, S> u(upd_base(R.raw(p, cb, 0), P.codec.raw(f_in, p * P.ps + c), c43, c13));
                     if (cx(p)) {
                         const int s = flux_slot(0, p);
-                        r = fma(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s], r);
+                        u.add(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s]);
                     }
                     if (cy(p)) {
                         const int s = flux_slot(1, p);
-                        r = fma(cy(p) > 0 ? -P.cyuf : P.cyuf, fy[s] - ysh[buf][wr - 1][s][lane], r);
+                        u.add(cy(p) > 0 ? -P.cyuf : P.cyuf, fy[s] - ysh[buf][wr - 1][s][lane]);
                     }
                     if (cz(p)) {
                         const int s = flux_slot(2, p);
-                        r = fma(cz(p) > 0 ? -P.czuf : P.czuf, fzu[s] - fzd[s], r);
+                        u.add(cz(p) > 0 ? -P.czuf : P.czuf, fzu[s] - fzd[s]);
                     }
-                    P.codec.store_h(f_out, p * P.ps + c, p, r, hc);
+                    f_out[p * P.ps + c] = u.encode(P.codec, p, hc);
                 }
             }
 #pragma unroll
@@ -1342,6 +1382,7 @@ struct SmemRead {
     }
     __device__ __forceinline__ T raw(int p, int row, int col) const { return codec.raw_s(ring, p * POPS + row + col); }
     __device__ __forceinline__ T dec(int p, T x) const { return codec.dec(p, x); }
+    __device__ __forceinline__ T dec_e(int p, T x) const { return codec.dec_e(p, x); }
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -1434,7 +1475,9 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
     // them in shared memory from the landed plane, g0 = q0 d(1) + (1-q0) d(2),
     // g_{nx+1} = q1 d(nx) + (1-q1) d(nx-1) (src/dugks.cu:1234-1251; stretched
     // mesh src/fortran/channel/src/dugks.cuf:365-374), on the stored deviations
-    // (the decode is affine) and rounded to the nearest 16-bit value.  Column 0
+    // (the decode is affine) and rounded as the engine rounds every stored value
+    // (stochastically, from the ghost cell's index; every tile that forms the
+    // same ghost gets the same value).  Column 0
     // is read only by the first tile, column nx+1 only by the tile holding nx.
     // (Formed by the whole CTA after each plane lands, with one more block
     // barrier in those tiles; done by the halo warp one plane ahead instead, it
@@ -1453,7 +1496,10 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
                 const int d = side ? -1 : 1;
                 const float q = side ? float(P.q1) : float(P.q0);
                 const float a = float(row[c + d]), b = float(row[c + 2 * d]);
-                row[c] = S(q * a + (1.0f - q) * b);
+                // rounded as a stored value of that ghost cell (stochastically, by its index)
+                const int p = seg / RD::RH, r = seg - p * RD::RH;
+                const long long dst = ((long long)g * (ny + 2) + (j0 - 1 + r)) * P.pitch_b + (i0 - 1 + c);
+                row[c] = P.codec.encode_dev(p * P.ps_b + dst, p, q * a + (1.0f - q) * b);
             }
         }
     };
@@ -1494,7 +1540,7 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
             if (cell) {
                 const long long c = ((long long)(k - 1) * ny + (gj - 1)) * P.pitch + (gi - 1);
 #pragma unroll
-                for (int p = 0; p < NPOP; ++p) fo[p] = P.codec.load(f_in, p * P.ps + c, p);
+                for (int p = 0; p < NPOP; ++p) fo[p] = P.codec.raw(f_in, p * P.ps + c);
             }
         } else {
             face_fluxes<T, S, 1, RECON, FF>(P, R, ci, j0 - 1, k, fy);
@@ -1524,20 +1570,20 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
                 const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
 #pragma unroll
                 for (int p = 0; p < NPOP; ++p) {
-                    T r = upd_base(R(p, cb, 0), fo[p], c43, c13);
+                    UpdateSum<T, S> u(upd_base(R.raw(p, cb, 0), fo[p], c43, c13));
                     if (cx(p)) {
                         const int s = flux_slot(0, p);
-                        r = fma(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s], r);
+                        u.add(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s]);
                     }
                     if (cy(p)) {
                         const int s = flux_slot(1, p);
-                        r = fma(cy(p) > 0 ? -P.cyuf : P.cyuf, fy[s] - ysh[buf][wr - 1][s][lane], r);
+                        u.add(cy(p) > 0 ? -P.cyuf : P.cyuf, fy[s] - ysh[buf][wr - 1][s][lane]);
                     }
                     if (cz(p)) {
                         const int s = flux_slot(2, p);
-                        r = fma(cz(p) > 0 ? -P.czuf : P.czuf, fzu[s] - fzd[s], r);
+                        u.add(cz(p) > 0 ? -P.czuf : P.czuf, fzu[s] - fzd[s]);
                     }
-                    P.codec.store_h(f_out, p * P.ps + c, p, r, hc);
+                    f_out[p * P.ps + c] = u.encode(P.codec, p, hc);
                 }
             }
 #pragma unroll

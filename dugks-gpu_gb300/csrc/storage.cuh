@@ -29,11 +29,16 @@ struct Codec {
     __device__ __forceinline__ void store(S *a, long long idx, int, T v) const { a[idx] = S(v); }
     __device__ __forceinline__ unsigned cell_hash(long long) const { return 0u; }
     __device__ __forceinline__ S encode_h(int, T v, unsigned) const { return S(v); }
+    __device__ __forceinline__ S encode_dh(int, T v, unsigned) const { return S(v); }
     __device__ __forceinline__ void store_h(S *a, long long idx, int p, T v, unsigned) const { store(a, idx, p, v); }
     // undecoded reads and the decode of a value affine in them (identity here)
     __device__ __forceinline__ T raw_nc(const S *a, long long idx) const { return T(__ldg(a + idx)); }
     __device__ __forceinline__ T raw_s(const S *a, int idx) const { return T(a[idx]); }
+    __device__ __forceinline__ T raw(const S *a, long long idx) const { return T(a[idx]); }
     __device__ __forceinline__ T dec(int, T x) const { return x; }
+    // the value less its rest-state equilibrium, as the flux kernels carry face
+    // values (plain forms: the value itself, the rest state is not removed)
+    __device__ __forceinline__ T dec_e(int, T x) const { return x; }
     static constexpr bool deviation = false;
 };
 
@@ -81,25 +86,30 @@ struct Codec<float, __half> : DevCodec<__half> {
         const float t = __uint_as_float((__float_as_uint(d) + r) & ~0x1fffu);
         return __float2half_rz(t);
     }
+    // deviation d rounded as the value stored at element idx (p: population)
+    __device__ __forceinline__ __half encode_dev(long long idx, int p, float d) const
+    {
+        if (sr_seed == 0) return __float2half_rn(d);
+        const unsigned r = mix32(unsigned(idx) * 19u + unsigned(p) + sr_seed * 0x9e3779b9u);
+        return sr_half(d, r & 0x1fffu);
+    }
     __device__ __forceinline__ void store(__half *a, long long idx, int p, float v) const
     {
-        const float d = (v - w[p]) * is[p];
-        if (sr_seed == 0) {
-            a[idx] = __float2half_rn(d);
-            return;
-        }
-        const unsigned r = mix32(unsigned(idx) * 19u + unsigned(p) + sr_seed * 0x9e3779b9u);
-        a[idx] = sr_half(d, r & 0x1fffu);
+        a[idx] = encode_dev(idx, p, (v - w[p]) * is[p]);
     }
     __device__ __forceinline__ unsigned cell_hash(long long cell) const
     {
         return sr_seed ? (mix32(unsigned(cell) ^ sr_seed) | 1u) : 0u;
     }
-    __device__ __forceinline__ __half encode_h(int p, float v, unsigned h) const
+    // deviation d stored with the cell hash h (0: round to nearest)
+    __device__ __forceinline__ __half encode_dh(int p, float d, unsigned h) const
     {
-        const float d = (v - w[p]) * is[p];
         if (h == 0u) return __float2half_rn(d);
         return sr_half(d, (h * (0x9e3779b1u + 0x6a09e66eu * unsigned(p))) >> 19);  // odd multiplier per p
+    }
+    __device__ __forceinline__ __half encode_h(int p, float v, unsigned h) const
+    {
+        return encode_dh(p, (v - w[p]) * is[p], h);
     }
     __device__ __forceinline__ void store_h(__half *a, long long idx, int p, float v, unsigned h) const
     {
@@ -108,6 +118,8 @@ struct Codec<float, __half> : DevCodec<__half> {
     __device__ __forceinline__ float raw_nc(const __half *a, long long idx) const { return __half2float(__ldg(a + idx)); }
     __device__ __forceinline__ float raw_s(const __half *a, int idx) const { return __half2float(a[idx]); }
     __device__ __forceinline__ float dec(int p, float x) const { return fmaf(s[p], x, w[p]); }
+    __device__ __forceinline__ float dec_e(int p, float x) const { return s[p] * x; }
+    __device__ __forceinline__ float raw(const __half *a, long long idx) const { return __half2float(a[idx]); }
 };
 
 template <>
@@ -124,28 +136,33 @@ struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
     {
         return fmaf(s[p], __bfloat162float(a[idx]), w[p]);
     }
-    __device__ __forceinline__ void store(__nv_bfloat16 *a, long long idx, int p, float v) const
+    // deviation d rounded as the value stored at element idx (p: population)
+    __device__ __forceinline__ __nv_bfloat16 encode_dev(long long idx, int p, float d) const
     {
-        const float d = (v - w[p]) * is[p];
-        if (sr_seed == 0) {
-            a[idx] = __float2bfloat16_rn(d);
-            return;
-        }
+        if (sr_seed == 0) return __float2bfloat16_rn(d);
         const unsigned r = mix32(unsigned(idx) * 19u + unsigned(p) + sr_seed * 0x9e3779b9u);
         const unsigned u = __float_as_uint(d) + (r & 0xffffu);  // magnitude rounds up with probability = fraction
-        a[idx] = __ushort_as_bfloat16((unsigned short)(u >> 16));
+        return __ushort_as_bfloat16((unsigned short)(u >> 16));
+    }
+    __device__ __forceinline__ void store(__nv_bfloat16 *a, long long idx, int p, float v) const
+    {
+        a[idx] = encode_dev(idx, p, (v - w[p]) * is[p]);
     }
     // per-cell hash of the step kernels (0: round to nearest)
     __device__ __forceinline__ unsigned cell_hash(long long cell) const
     {
         return sr_seed ? (mix32(unsigned(cell) ^ sr_seed) | 1u) : 0u;
     }
-    __device__ __forceinline__ __nv_bfloat16 encode_h(int p, float v, unsigned h) const
+    // deviation d stored with the cell hash h (0: round to nearest)
+    __device__ __forceinline__ __nv_bfloat16 encode_dh(int p, float d, unsigned h) const
     {
-        const float d = (v - w[p]) * is[p];
         if (h == 0u) return __float2bfloat16_rn(d);
         const unsigned r = (h * (0x9e3779b1u + 0x6a09e66eu * unsigned(p))) >> 16;  // odd multiplier per p
         return __ushort_as_bfloat16((unsigned short)((__float_as_uint(d) + r) >> 16));
+    }
+    __device__ __forceinline__ __nv_bfloat16 encode_h(int p, float v, unsigned h) const
+    {
+        return encode_dh(p, (v - w[p]) * is[p], h);
     }
     __device__ __forceinline__ void store_h(__nv_bfloat16 *a, long long idx, int p, float v, unsigned h) const
     {
@@ -157,6 +174,8 @@ struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
     }
     __device__ __forceinline__ float raw_s(const __nv_bfloat16 *a, int idx) const { return __bfloat162float(a[idx]); }
     __device__ __forceinline__ float dec(int p, float x) const { return fmaf(s[p], x, w[p]); }
+    __device__ __forceinline__ float dec_e(int p, float x) const { return s[p] * x; }
+    __device__ __forceinline__ float raw(const __nv_bfloat16 *a, long long idx) const { return __bfloat162float(a[idx]); }
 };
 
 }  // namespace dg
