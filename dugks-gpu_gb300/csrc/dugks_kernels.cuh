@@ -620,6 +620,7 @@ struct FbRead {
         return codec.load_nc(fb, p * ps + row + col, p);
     }
     __device__ __forceinline__ T raw(int p, long long row, int col) const { return codec.raw_nc(fb, p * ps + row + col); }
+    __device__ __forceinline__ S bits(int p, long long row, int col) const { return __ldg(fb + p * ps + row + col); }
     __device__ __forceinline__ T dec(int p, T x) const { return codec.dec(p, x); }
     __device__ __forceinline__ T dec_e(int p, T x) const { return codec.dec_e(p, x); }
 };
@@ -781,6 +782,40 @@ __device__ __forceinline__ float2 lerp_x2(float2 om, float2 m, float2 a, float2 
     return __ffma2_rn(m, b, __fmul2_rn(om, a));
 }
 
+// b - a for a stored 16-bit value b and a float a, in one mixed-precision
+// subtraction (sm_100+: the 16-bit operand is widened exactly inside the
+// instruction, the difference rounded once to FP32).
+__device__ __forceinline__ float sub_stored(__half b, float a)
+{
+    float d;
+    asm("sub.rn.f32.f16 %0, %1, %2;" : "=f"(d) : "h"(__half_as_ushort(b)), "f"(a));
+    return d;
+}
+__device__ __forceinline__ float sub_stored(__nv_bfloat16 b, float a)
+{
+    float d;
+    asm("sub.rn.f32.bf16 %0, %1, %2;" : "=f"(d) : "h"(__bfloat16_as_ushort(b)), "f"(a));
+    return d;
+}
+
+// First lerp of a stencil, between two stored values of each of the pair
+// (a = (ap, aq) weighted om, b = (bp, bq) weighted m).  FP32: lerp_x2.  16-bit
+// forms: a + m (b - a), a widened and b - a taken by sub_stored (three
+// instructions per pair of values instead of four widenings and two packed
+// products); this uses om = 1 - m, which the weight tables hold to the last
+// bit of FP32.
+template <class S>
+__device__ __forceinline__ float2 lerp_first_x2(float2 om, float2 m, S ap, S aq, S bp, S bq)
+{
+    if constexpr (sizeof(S) == 2) {
+        const float2 af = make_float2(float(ap), float(aq));
+        return __ffma2_rn(m, make_float2(sub_stored(bp, af.x), sub_stored(bq, af.y)), af);
+    } else {
+        (void)om;
+        return lerp_x2(om, m, make_float2(ap, aq), make_float2(bp, bq));
+    }
+}
+
 template <class S, int AX, class RD>
 __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const RD &R, int i, int j, int k,
                                             float v[NPOP])
@@ -791,6 +826,12 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
     const int xs = P.xws;
     const float2 ty_o = make_float2(P.ty_om, P.ty_om), ty_m = make_float2(P.ty_m, P.ty_m);
     const float2 tz_o = make_float2(P.tz_om, P.tz_om), tz_m = make_float2(P.tz_m, P.tz_m);
+    // first lerp of populations p, q between (row ra, column ca) and (row rb, column cb) of each
+    auto L1 = [&](float2 om, float2 m, int p, int q, RI rap, int cap, RI raq, int caq, RI rbp, int cbp, RI rbq,
+                  int cbq) {
+        return lerp_first_x2<S>(om, m, R.bits(p, rap, cap), R.bits(q, raq, caq), R.bits(p, rbp, cbp),
+                                R.bits(q, rbq, cbq));
+    };
     if (AX == 0) {
         const int A = i == 0 ? 1 : i, B = i == 0 ? 0 : i + 1;
         const float *xw = P.xw + i;
@@ -807,25 +848,21 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
             const float2 om = xrep(p) == 3 ? om33 : om12, m = xrep(p) == 3 ? m33 : m12;
             const int jtp = cy(p) > 0 ? jm : (cy(p) < 0 ? jp : jc), jtq = cy(q) > 0 ? jm : (cy(q) < 0 ? jp : jc);
             const int ktp = cz(p) > 0 ? km : (cz(p) < 0 ? kp : kc), ktq = cz(q) > 0 ? km : (cz(q) < 0 ? kp : kc);
-            const float2 x00 = lerp_x2(om, m, make_float2(R.raw(p, r00, A), R.raw(q, r00, A)),
-                                       make_float2(R.raw(p, r00, B), R.raw(q, r00, B)));
+            const float2 x00 = L1(om, m, p, q, r00, A, r00, A, r00, B, r00, B);
             float2 y00 = x00;
             if (ay) {
                 const RI sp = R.rb(jtp, kc), sq = R.rb(jtq, kc);
-                const float2 x01 = lerp_x2(om, m, make_float2(R.raw(p, sp, A), R.raw(q, sq, A)),
-                                           make_float2(R.raw(p, sp, B), R.raw(q, sq, B)));
+                const float2 x01 = L1(om, m, p, q, sp, A, sq, A, sp, B, sq, B);
                 y00 = lerp_x2(ty_o, ty_m, x00, x01);
             }
             float2 res = y00;
             if (az) {
                 const RI tp = R.rb(jc, ktp), tq = R.rb(jc, ktq);
-                const float2 x10 = lerp_x2(om, m, make_float2(R.raw(p, tp, A), R.raw(q, tq, A)),
-                                           make_float2(R.raw(p, tp, B), R.raw(q, tq, B)));
+                const float2 x10 = L1(om, m, p, q, tp, A, tq, A, tp, B, tq, B);
                 float2 y11 = x10;
                 if (ay) {
                     const RI up = R.rb(jtp, ktp), uq = R.rb(jtq, ktq);
-                    const float2 x11 = lerp_x2(om, m, make_float2(R.raw(p, up, A), R.raw(q, uq, A)),
-                                               make_float2(R.raw(p, up, B), R.raw(q, uq, B)));
+                    const float2 x11 = L1(om, m, p, q, up, A, uq, A, up, B, uq, B);
                     y11 = lerp_x2(ty_o, ty_m, x10, x11);
                 }
                 res = lerp_x2(tz_o, tz_m, y00, y11);
@@ -847,23 +884,20 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
             const int iop = i - cx(p), ioq = i - cx(q);
             const int ktp = cz(p) > 0 ? km : (cz(p) < 0 ? kp : kc), ktq = cz(q) > 0 ? km : (cz(q) < 0 ? kp : kc);
             const float2 yo = make_float2(P.yn_om[p], P.yn_om[q]), ym = make_float2(P.yn_m[p], P.yn_m[q]);
-            float2 x00 = make_float2(R.raw(p, rA, i), R.raw(q, rA, i));
-            float2 x01 = make_float2(R.raw(p, rB, i), R.raw(q, rB, i));
-            if (ax) {
-                x00 = lerp_x2(tx_o, tx_m, x00, make_float2(R.raw(p, rA, iop), R.raw(q, rA, ioq)));
-                x01 = lerp_x2(tx_o, tx_m, x01, make_float2(R.raw(p, rB, iop), R.raw(q, rB, ioq)));
-            }
-            const float2 y00 = lerp_x2(yo, ym, x00, x01);
+            // normal lerp between rows A and B of the values at column i, x-lerped first when c_x != 0
+            auto yl = [&](RI sAp, RI sAq, RI sBp, RI sBq) {
+                if (ax) {
+                    const float2 x0 = L1(tx_o, tx_m, p, q, sAp, i, sAq, i, sAp, iop, sAq, ioq);
+                    const float2 x1 = L1(tx_o, tx_m, p, q, sBp, i, sBq, i, sBp, iop, sBq, ioq);
+                    return lerp_x2(yo, ym, x0, x1);
+                }
+                return L1(yo, ym, p, q, sAp, i, sAq, i, sBp, i, sBq, i);
+            };
+            const float2 y00 = yl(rA, rA, rB, rB);
             float2 res = y00;
             if (az) {
                 const RI sAp = R.rb(jc, ktp), sBp = R.rb(jp, ktp), sAq = R.rb(jc, ktq), sBq = R.rb(jp, ktq);
-                float2 x10 = make_float2(R.raw(p, sAp, i), R.raw(q, sAq, i));
-                float2 x11 = make_float2(R.raw(p, sBp, i), R.raw(q, sBq, i));
-                if (ax) {
-                    x10 = lerp_x2(tx_o, tx_m, x10, make_float2(R.raw(p, sAp, iop), R.raw(q, sAq, ioq)));
-                    x11 = lerp_x2(tx_o, tx_m, x11, make_float2(R.raw(p, sBp, iop), R.raw(q, sBq, ioq)));
-                }
-                res = lerp_x2(tz_o, tz_m, y00, lerp_x2(yo, ym, x10, x11));
+                res = lerp_x2(tz_o, tz_m, y00, yl(sAp, sAq, sBp, sBq));
             }
             v[p] = R.dec_e(p, res.x);
             v[q] = R.dec_e(q, res.y);
@@ -882,25 +916,30 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
             const int iop = i - cx(p), ioq = i - cx(q);
             const int jtp = cy(p) > 0 ? jm : (cy(p) < 0 ? jp : jc), jtq = cy(q) > 0 ? jm : (cy(q) < 0 ? jp : jc);
             const float2 zo = make_float2(P.zn_om[p], P.zn_om[q]), zm = make_float2(P.zn_m[p], P.zn_m[q]);
-            float2 x00 = make_float2(R.raw(p, rA, i), R.raw(q, rA, i));
-            float2 x10 = make_float2(R.raw(p, rB, i), R.raw(q, rB, i));
-            if (ax) {
-                x00 = lerp_x2(tx_o, tx_m, x00, make_float2(R.raw(p, rA, iop), R.raw(q, rA, ioq)));
-                x10 = lerp_x2(tx_o, tx_m, x10, make_float2(R.raw(p, rB, iop), R.raw(q, rB, ioq)));
-            }
-            float2 y00 = x00, y11 = x10;
-            if (ay) {
-                const RI sAp = R.rb(jtp, kc), sBp = R.rb(jtp, kp), sAq = R.rb(jtq, kc), sBq = R.rb(jtq, kp);
-                float2 x01 = make_float2(R.raw(p, sAp, i), R.raw(q, sAq, i));
-                float2 x11 = make_float2(R.raw(p, sBp, i), R.raw(q, sBq, i));
-                if (ax) {
-                    x01 = lerp_x2(tx_o, tx_m, x01, make_float2(R.raw(p, sAp, iop), R.raw(q, sAq, ioq)));
-                    x11 = lerp_x2(tx_o, tx_m, x11, make_float2(R.raw(p, sBp, iop), R.raw(q, sBq, ioq)));
+            // value at column i of rows sp / sq, x-lerped when c_x != 0 (first lerps)
+            auto xl = [&](RI sp, RI sq) {
+                return L1(tx_o, tx_m, p, q, sp, i, sq, i, sp, iop, sq, ioq);
+            };
+            float2 res;
+            if (!ax && !ay) {
+                res = L1(zo, zm, p, q, rA, i, rA, i, rB, i, rB, i);
+            } else {
+                float2 y00, y11;
+                if (ay) {
+                    const RI sAp = R.rb(jtp, kc), sBp = R.rb(jtp, kp), sAq = R.rb(jtq, kc), sBq = R.rb(jtq, kp);
+                    if (ax) {
+                        y00 = lerp_x2(ty_o, ty_m, xl(rA, rA), xl(sAp, sAq));
+                        y11 = lerp_x2(ty_o, ty_m, xl(rB, rB), xl(sBp, sBq));
+                    } else {
+                        y00 = L1(ty_o, ty_m, p, q, rA, i, rA, i, sAp, i, sAq, i);
+                        y11 = L1(ty_o, ty_m, p, q, rB, i, rB, i, sBp, i, sBq, i);
+                    }
+                } else {
+                    y00 = xl(rA, rA);
+                    y11 = xl(rB, rB);
                 }
-                y00 = lerp_x2(ty_o, ty_m, x00, x01);
-                y11 = lerp_x2(ty_o, ty_m, x10, x11);
+                res = lerp_x2(zo, zm, y00, y11);
             }
-            const float2 res = lerp_x2(zo, zm, y00, y11);
             v[p] = R.dec_e(p, res.x);
             v[q] = R.dec_e(q, res.y);
         }
@@ -1247,8 +1286,8 @@ __device__ __forceinline__ void face_fluxes(const StepParams<T, S> &P, const RD 
     T v[NPOP];
     if constexpr (RECON == 0 && Fp64Form<T>::value)
         face_tri_cw<T, S, AX>(P, R, i, j, k, v);
-    else if constexpr (RECON == 0 && (std::is_same<S, float>::value || std::is_same<S, __nv_bfloat16>::value))
-        face_tri_x2<S, AX>(P, R, i, j, k, v);  // packed lerps: FP32 and BF16 (FP16 measured 3 % slower packed)
+    else if constexpr (RECON == 0 && std::is_same<T, float>::value)
+        face_tri_x2<S, AX>(P, R, i, j, k, v);  // packed lerps: FP32, FP16, BF16
     else if constexpr (RECON == 0)
         face_tri<T, S, AX>(P, R, i, j, k, v);
     else
@@ -1381,6 +1420,7 @@ struct SmemRead {
         return codec.load_s(ring, p * POPS + row + col, p);
     }
     __device__ __forceinline__ T raw(int p, int row, int col) const { return codec.raw_s(ring, p * POPS + row + col); }
+    __device__ __forceinline__ S bits(int p, int row, int col) const { return ring[p * POPS + row + col]; }
     __device__ __forceinline__ T dec(int p, T x) const { return codec.dec(p, x); }
     __device__ __forceinline__ T dec_e(int p, T x) const { return codec.dec_e(p, x); }
 };
