@@ -164,6 +164,34 @@ __device__ __forceinline__ void moments(const T v[NPOP], T &r, T &jx, T &jy, T &
     jz = ((d5 + d11) + d12) + (d15 + d16);
 }
 
+// moments for FP32 arithmetic on the population pairs (2m-1, 2m), m = 1..9, as
+// packed FP32x2 sums (sm_100+ FADD2/FFMA2): rho from the nine pairs summed
+// pairwise, each momentum component from the pairs that move along it, whose
+// c pattern within a pair is (+, -), (+, +) or (-, -) -- 27 operations instead
+// of 39 (same values to rounding).
+__device__ __forceinline__ float2 sub_x2(float2 a, float2 b)
+{
+    return __ffma2_rn(b, make_float2(-1.0f, -1.0f), a);  // a - b, one rounding
+}
+__device__ __forceinline__ void moments_x2(const float v[NPOP], float &r, float &jx, float &jy, float &jz)
+{
+    auto V = [&](int m) { return make_float2(v[2 * m - 1], v[2 * m]); };
+    const float2 a = __fadd2_rn(__fadd2_rn(V(1), V(2)), __fadd2_rn(V(3), V(4)));
+    const float2 b = __fadd2_rn(__fadd2_rn(V(5), V(6)), __fadd2_rn(V(7), V(8)));
+    const float2 sr = __fadd2_rn(__fadd2_rn(a, b), V(9));
+    r = v[0] + (sr.x + sr.y);
+    // x: pairs 1, 4, 5, 6, 7 are (+, -)
+    const float2 X = __fadd2_rn(__fadd2_rn(V(1), V(4)), __fadd2_rn(__fadd2_rn(V(5), V(6)), V(7)));
+    jx = X.x - X.y;
+    // y: pairs 2, 8, 9 (+, -); 4 (+, +); 5 (-, -)
+    const float2 Y1 = __fadd2_rn(__fadd2_rn(V(2), V(8)), V(9)), Y2 = sub_x2(V(4), V(5));
+    jy = (Y1.x - Y1.y) + (Y2.x + Y2.y);
+    // z: pair 3 (+, -); 6, 8 (+, +); 7, 9 (-, -)
+    const float2 Z = sub_x2(__fadd2_rn(V(6), V(8)), __fadd2_rn(V(7), V(9)));
+    const float2 V3 = V(3);
+    jz = (V3.x - V3.y) + (Z.x + Z.y);
+}
+
 // 1/r: FP64 from a single-precision seed x (relative error e ~ 2^-23) and one
 // third-order correction x (1 + e + e^2) (truncation error ~e^3, far below the
 // rounding level): three dependent FMAs, cheaper than the full-precision
@@ -214,6 +242,53 @@ struct UpdateSum {
             return c.encode_dh(p, nt ? fma(c.is[p], acc, r) : r, hc);
         else
             return c.encode_h(p, r, hc);
+    }
+};
+
+// UpdateSum for the population pair (2m-1, 2m) in FP32 arithmetic, two at a
+// time (FFMA2 / FMUL2): the same operations in the same order for each.
+// The update's pairing rule: the pair (2m-1, 2m) moves along the same axes
+// and sits in adjacent slots of each of their flux lists.
+__host__ __device__ constexpr bool update_pairs_ok()
+{
+    for (int m = 1; m <= 9; ++m) {
+        const int p = 2 * m - 1, q = 2 * m;
+        for (int a = 0; a < 3; ++a) {
+            if ((cc(a, p) != 0) != (cc(a, q) != 0)) return false;
+            if (cc(a, p) != 0 && flux_slot(a, q) != flux_slot(a, p) + 1) return false;
+        }
+    }
+    return true;
+}
+static_assert(update_pairs_ok(), "update population pairs must share their axes and adjacent flux slots");
+
+template <class S>
+struct UpdatePair {
+    float2 r, acc = make_float2(0.0f, 0.0f);
+    int nt = 0;
+    __device__ __forceinline__ explicit UpdatePair(float2 fb, float2 fo)
+        : r(__ffma2_rn(__ffma2_rn(fo, make_float2(-1.0f, -1.0f), fb), make_float2(1.0f / 3.0f, 1.0f / 3.0f), fb))
+    {
+    }  // upd_base, FP32 form: fb + (fb - fo) / 3
+    __device__ __forceinline__ void add(float2 coef, float2 diff)
+    {
+        if constexpr (Codec<float, S>::deviation)
+            acc = nt ? __ffma2_rn(coef, diff, acc) : __fmul2_rn(coef, diff);
+        else
+            r = __ffma2_rn(coef, diff, r);
+        ++nt;
+    }
+    __device__ __forceinline__ void store(const Codec<float, S> &c, S *out, long long ip, long long iq, int p, int q,
+                                          unsigned hc) const
+    {
+        if constexpr (Codec<float, S>::deviation) {
+            const float2 d = nt ? __ffma2_rn(make_float2(c.is[p], c.is[q]), acc, r) : r;
+            out[ip] = c.encode_dh(p, d.x, hc);
+            out[iq] = c.encode_dh(q, d.y, hc);
+        } else {
+            out[ip] = c.encode_h(p, r.x, hc);
+            out[iq] = c.encode_h(q, r.y, hc);
+        }
     }
 };
 
@@ -623,6 +698,7 @@ struct FbRead {
     __device__ __forceinline__ S bits(int p, long long row, int col) const { return __ldg(fb + p * ps + row + col); }
     __device__ __forceinline__ T dec(int p, T x) const { return codec.dec(p, x); }
     __device__ __forceinline__ T dec_e(int p, T x) const { return codec.dec_e(p, x); }
+    __device__ __forceinline__ float2 dec_e2(int p, int q, float2 x) const { return codec.dec_e2(p, q, x); }
 };
 
 // 19 reconstructed values of one face, trilinear characteristic interpolation
@@ -867,8 +943,9 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
                 }
                 res = lerp_x2(tz_o, tz_m, y00, y11);
             }
-            v[p] = R.dec_e(p, res.x);
-            v[q] = R.dec_e(q, res.y);
+            const float2 e = R.dec_e2(p, q, res);
+            v[p] = e.x;
+            v[q] = e.y;
         }
     } else if (AX == 1) {
         // rows j (A) and j+1 (B); transverse x to column i - cx, z to plane k - cz
@@ -899,8 +976,9 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
                 const RI sAp = R.rb(jc, ktp), sBp = R.rb(jp, ktp), sAq = R.rb(jc, ktq), sBq = R.rb(jp, ktq);
                 res = lerp_x2(tz_o, tz_m, y00, yl(sAp, sAq, sBp, sBq));
             }
-            v[p] = R.dec_e(p, res.x);
-            v[q] = R.dec_e(q, res.y);
+            const float2 e = R.dec_e2(p, q, res);
+            v[p] = e.x;
+            v[q] = e.y;
         }
     } else {
         // planes k (A) and k+1 (B); transverse x to column i - cx, y to row j - cy
@@ -940,8 +1018,9 @@ __device__ __forceinline__ void face_tri_x2(const StepParams<float, S> &P, const
                 }
                 res = lerp_x2(zo, zm, y00, y11);
             }
-            v[p] = R.dec_e(p, res.x);
-            v[q] = R.dec_e(q, res.y);
+            const float2 e = R.dec_e2(p, q, res);
+            v[p] = e.x;
+            v[q] = e.y;
         }
     }
 }
@@ -1163,7 +1242,10 @@ template <class T, class S, int AX, bool FF>
 __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[NPOP], T out[10], T fadd)
 {
     T r, jx, jy, jz;
-    moments(v, r, jx, jy, jz);
+    if constexpr (std::is_same<T, float>::value)
+        moments_x2(v, r, jx, jy, jz);
+    else
+        moments(v, r, jx, jy, jz);
     // 16-bit forms: v holds f_p - w_p; the rest state adds sum w_p = 1 to the
     // density and nothing to the momentum, and out carries F_p - w_p, which the
     // update only differences between the two faces of a cell
@@ -1231,15 +1313,31 @@ __device__ __forceinline__ void face_flux(const StepParams<T, S> &P, const T v[N
         }
         return;
     }
-#pragma unroll
-    for (int s = 0; s < 10; ++s) {
-        const int p = flux_pop(AX, s);
+    auto coef = [&](int p) {
         T K = P.Kfs[p];
         if (FF) {
             const int ca = P.ffaxis == 0 ? cx(p) : (P.ffaxis == 1 ? cy(p) : cz(p));
             if (ca) K = fma(ca > 0 ? P.fw0x3s : -P.fw0x3s, fadd, K);
         }
-        out[s] = fma(B + K, fe[p], v[p]);
+        return K;
+    };
+    if constexpr (std::is_same<T, float>::value) {
+        // slots (2t, 2t+1) hold the pair (2m-1, 2m): the same operations two at a time
+        const float2 B2 = make_float2(B, B);
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+            const int p = flux_pop(AX, 2 * t), q = flux_pop(AX, 2 * t + 1);
+            const float2 o = __ffma2_rn(__fadd2_rn(B2, make_float2(coef(p), coef(q))), make_float2(fe[p], fe[q]),
+                                        make_float2(v[p], v[q]));
+            out[2 * t] = o.x;
+            out[2 * t + 1] = o.y;
+        }
+    } else {
+#pragma unroll
+        for (int s = 0; s < 10; ++s) {
+            const int p = flux_pop(AX, s);
+            out[s] = fma(B + coef(p), fe[p], v[p]);
+        }
     }
 }
 
@@ -1423,6 +1521,7 @@ struct SmemRead {
     __device__ __forceinline__ S bits(int p, int row, int col) const { return ring[p * POPS + row + col]; }
     __device__ __forceinline__ T dec(int p, T x) const { return codec.dec(p, x); }
     __device__ __forceinline__ T dec_e(int p, T x) const { return codec.dec_e(p, x); }
+    __device__ __forceinline__ float2 dec_e2(int p, int q, float2 x) const { return codec.dec_e2(p, q, x); }
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -1608,22 +1707,34 @@ __global__ void __launch_bounds__(32 * W, MINB) flux_tma_kernel(const __grid_con
                 const int cb = R.rb(gj, k) + gi;
                 const T cxg = __ldg(P.cxuf + gi);
                 const T c43 = T(4.0 / 3.0), c13 = T(1.0 / 3.0);
+                {
+                    const UpdateSum<T, S> u(upd_base(R.raw(0, cb, 0), fo[0], c43, c13));  // rest population
+                    f_out[c] = u.encode(P.codec, 0, hc);
+                }
+                // the pairs (2m-1, 2m): they move along the same axes, and their flux
+                // slots along each are adjacent
+                auto sgn = [](int a, T cval) { return a > 0 ? -cval : cval; };
 #pragma unroll
-                for (int p = 0; p < NPOP; ++p) {
-                    UpdateSum<T, S> u(upd_base(R.raw(p, cb, 0), fo[p], c43, c13));
+                for (int m = 1; m <= 9; ++m) {
+                    const int p = 2 * m - 1, q = 2 * m;
+                    UpdatePair<S> u(make_float2(R.raw(p, cb, 0), R.raw(q, cb, 0)), make_float2(fo[p], fo[q]));
                     if (cx(p)) {
                         const int s = flux_slot(0, p);
-                        u.add(cx(p) > 0 ? -cxg : cxg, fx[s] - fxl[s]);
+                        u.add(make_float2(sgn(cx(p), cxg), sgn(cx(q), cxg)),
+                              sub_x2(make_float2(fx[s], fx[s + 1]), make_float2(fxl[s], fxl[s + 1])));
                     }
                     if (cy(p)) {
                         const int s = flux_slot(1, p);
-                        u.add(cy(p) > 0 ? -P.cyuf : P.cyuf, fy[s] - ysh[buf][wr - 1][s][lane]);
+                        u.add(make_float2(sgn(cy(p), P.cyuf), sgn(cy(q), P.cyuf)),
+                              sub_x2(make_float2(fy[s], fy[s + 1]),
+                                     make_float2(ysh[buf][wr - 1][s][lane], ysh[buf][wr - 1][s + 1][lane])));
                     }
                     if (cz(p)) {
                         const int s = flux_slot(2, p);
-                        u.add(cz(p) > 0 ? -P.czuf : P.czuf, fzu[s] - fzd[s]);
+                        u.add(make_float2(sgn(cz(p), P.czuf), sgn(cz(q), P.czuf)),
+                              sub_x2(make_float2(fzu[s], fzu[s + 1]), make_float2(fzd[s], fzd[s + 1])));
                     }
-                    f_out[p * P.ps + c] = u.encode(P.codec, p, hc);
+                    u.store(P.codec, f_out, p * P.ps + c, q * P.ps + c, p, q, hc);
                 }
             }
 #pragma unroll

@@ -39,6 +39,7 @@ struct Codec {
     // the value less its rest-state equilibrium, as the flux kernels carry face
     // values (plain forms: the value itself, the rest state is not removed)
     __device__ __forceinline__ T dec_e(int, T x) const { return x; }
+    __device__ __forceinline__ float2 dec_e2(int, int, float2 x) const { return x; }
     static constexpr bool deviation = false;
 };
 
@@ -119,6 +120,10 @@ struct Codec<float, __half> : DevCodec<__half> {
     __device__ __forceinline__ float raw_s(const __half *a, int idx) const { return __half2float(a[idx]); }
     __device__ __forceinline__ float dec(int p, float x) const { return fmaf(s[p], x, w[p]); }
     __device__ __forceinline__ float dec_e(int p, float x) const { return s[p] * x; }
+    __device__ __forceinline__ float2 dec_e2(int p, int q, float2 x) const
+    {
+        return __fmul2_rn(make_float2(s[p], s[q]), x);
+    }
     __device__ __forceinline__ float raw(const __half *a, long long idx) const { return __half2float(a[idx]); }
 };
 
@@ -175,6 +180,10 @@ struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
     __device__ __forceinline__ float raw_s(const __nv_bfloat16 *a, int idx) const { return __bfloat162float(a[idx]); }
     __device__ __forceinline__ float dec(int p, float x) const { return fmaf(s[p], x, w[p]); }
     __device__ __forceinline__ float dec_e(int p, float x) const { return s[p] * x; }
+    __device__ __forceinline__ float2 dec_e2(int p, int q, float2 x) const
+    {
+        return __fmul2_rn(make_float2(s[p], s[q]), x);
+    }
     __device__ __forceinline__ float raw(const __nv_bfloat16 *a, long long idx) const { return __bfloat162float(a[idx]); }
 };
 
