@@ -45,6 +45,15 @@ __host__ __device__ constexpr T weight(int p)
     return p == 0 ? T(1.0 / 3.0) : (p <= 6 ? T(1.0 / 18.0) : T(1.0 / 36.0));
 }
 
+// 19 per-population values with population 1 at an 8-byte boundary, so that
+// each pair (2m-1, 2m) of the packed FP32x2 code is one aligned 8-byte word
+template <class T>
+struct alignas(8) PopArr {
+    T pad_, v[NPOP];
+    __host__ __device__ T &operator[](int p) { return v[p]; }
+    __host__ __device__ const T &operator[](int p) const { return v[p]; }
+};
+
 // The 10 populations that cross a face normal to `axis` (c_axis != 0), in
 // ascending order; the flux of a face is stored for these only.
 __host__ __device__ constexpr int flux_pop(int axis, int s)

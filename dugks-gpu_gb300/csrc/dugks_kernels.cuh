@@ -3,16 +3,18 @@
 // Layout in HBM: structure of arrays, one plane per population.
 //   f-tilde:         f[p*ps + ((k*ny + j)*pitch + i)]           (0-based i, j, k; interior only)
 //   f-bar-plus:     fb[p*ps_b + (((k+1)*(ny+2) + j+1)*pitch_b + i + 1)]
-//                   with one ghost layer on every side, written by
-//                   fb_ghost_kernel (periodic images, wall extrapolation);
-//                   this replaces the reference's extend_fb_x / extend_fb_x_wall /
-//                   extend_fb_y kernels and the MPI z exchange
-//                   (src/dugks.cu:348-377, src/parallel.cu:185-234).
+//                   with one ghost layer on every side (periodic images, wall
+//                   extrapolation), which replaces the reference's extend_fb_x /
+//                   extend_fb_x_wall / extend_fb_y kernels and the MPI z exchange
+//                   (src/dugks.cu:348-377, src/parallel.cu:185-234): written by
+//                   fb_ghost_kernel (FP64; 16-bit forms with periodic x), by
+//                   fbar_kernel itself (FP32; 16-bit forms between walls: the y / z
+//                   images, the wall columns formed by the flux kernel in shared memory).
 //
 // Kernels:
-//   fbar_kernel      stage (a), src/dugks.cu:1131-1196 (calc_fb1); in the FP32 form
-//                    also the ghost layer of f-bar-plus
-//   fb_ghost_kernel  x ghost columns of f-bar-plus (periodic images / wall extrapolation)
+//   fbar_kernel      stage (a), src/dugks.cu:1131-1196 (calc_fb1), with or without
+//                    the ghost writes
+//   fb_ghost_kernel  the ghost layer of f-bar-plus in a separate pass
 //   flux_kernel      stages (c) (d) (e), src/dugks.cu:715-959 (calc_fx_tri) or the
 //                    central-difference variant 421-649 (calc_fx); every face
 //                    evaluated once, z-marching warp rows
@@ -78,20 +80,21 @@ struct StepParams {
     // stage (a)
     T hdt, bw1, bw2, bw0x3;      // bw0x3 = 3*bw0
     T F[3];                      // ambient force
-    T Kb[NPOP];                  // 3*bw0*(c_p . F)
+    PopArr<T> Kb;                // 3*bw0*(c_p . F)
     T Fa, hFa, Kba, Kfa;         // fax >= 0: F, (0.5*hdt)*F, Kb, Kfs of the force axis (c_p = +1 on it)
     // faces
     T fw1, fw2, fw0x3;           // fw0x3 = 3*fw0
     T hF[3];                     // (0.5*hdt)*F, the face velocity shift (src/dugks.cu:698-700)
     T Kf[NPOP];                  // 3*fw0*(c_p . F)
-    T fw2s, fw0x3s, Kfs[NPOP];   // fw2, 3*fw0, Kf divided by fw1 (fluxes are kept divided by fw1)
+    T fw2s, fw0x3s;              // fw2, 3*fw0 divided by fw1 (fluxes are kept divided by fw1)
+    PopArr<T> Kfs;               // Kf divided by fw1
     T bwF;                       // bw2*hdt + bw0: momentum of f-bar-plus = j + rho F bwF (exact arithmetic)
     T cyuf, czuf;                // fw1*dt/dy, fw1*dt/dz
     // interpolation weights, (1-m, m) pairs in the reference's lerp form
     T ty_om, ty_m;               // transverse y, |hdt/dy|
     T tz_om, tz_m;               // transverse z, |hdt/dz|
-    T yn_om[NPOP], yn_m[NPOP];   // y-face normal (dy/2 - hdt*cy)/dy
-    T zn_om[NPOP], zn_m[NPOP];   // z-face normal (dz/2 - hdt*cz)/dz
+    PopArr<T> yn_om, yn_m;       // y-face normal (dy/2 - hdt*cy)/dy
+    PopArr<T> zn_om, zn_m;       // z-face normal (dz/2 - hdt*cz)/dz
     T cyu, czu;                  // dt/dy, dt/dz
     T q0, q1;                    // wall ghost extrapolation weights (2 on a uniform mesh)
     T g_idx, g_idy, g_idz;       // gradient reconstruction: 1/dx, 1/dy, 1/dz
@@ -456,11 +459,26 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     const long long cb = ((long long)(k + 1) * (ny + 2) + (j + 1)) * P.pitch_b + ic + 1;
 
     T v[NPOP];
+    if constexpr (Codec<T, S>::deviation) {
+        // decoded two populations at a time (pairs 2m-1, 2m)
+        v[0] = P.codec.load_nc(f, c, 0);
 #pragma unroll
-    for (int p = 0; p < NPOP; ++p) v[p] = P.codec.load_nc(f, p * P.ps + c, p);
+        for (int m = 1; m <= 9; ++m) {
+            const int p = 2 * m - 1, q = 2 * m;
+            const float2 x = P.codec.dec2(p, q, make_float2(P.codec.raw_nc(f, p * P.ps + c), P.codec.raw_nc(f, q * P.ps + c)));
+            v[p] = x.x;
+            v[q] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) v[p] = P.codec.load_nc(f, p * P.ps + c, p);
+    }
 
     T r, jx, jy, jz;
-    moments(v, r, jx, jy, jz);
+    if constexpr (std::is_same<T, float>::value)
+        moments_x2(v, r, jx, jy, jz);
+    else
+        moments(v, r, jx, jy, jz);
     const T inv = recip(r);
     T u = jx * inv, vv = jy * inv, w = jz * inv;
 
@@ -500,8 +518,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     } else {
         T fe[NPOP];
         feq_all(r, u, vv, w, fe);
-#pragma unroll
-        for (int p = 0; p < NPOP; ++p) {
+        auto kcoef = [&](int p) {
             T K = P.Kb[p];
             if (P.perturb || P.ffield) {
                 T cf = T(0);
@@ -510,7 +527,23 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
                 if (cz(p)) cf += cz(p) > 0 ? Fz : -Fz;
                 K = P.bw0x3 * cf;
             }
-            ob[p] = fma(B + K, fe[p], P.bw1 * v[p]);
+            return K;
+        };
+        if constexpr (std::is_same<T, float>::value) {
+            // the same operations on the pairs (2m-1, 2m), two at a time
+            ob[0] = fma(B + kcoef(0), fe[0], P.bw1 * v[0]);
+            const float2 B2 = make_float2(B, B), bw = make_float2(P.bw1, P.bw1);
+#pragma unroll
+            for (int m = 1; m <= 9; ++m) {
+                const int p = 2 * m - 1, q = 2 * m;
+                const float2 o = __ffma2_rn(__fadd2_rn(B2, make_float2(kcoef(p), kcoef(q))), make_float2(fe[p], fe[q]),
+                                            __fmul2_rn(bw, make_float2(v[p], v[q])));
+                ob[p] = o.x;
+                ob[q] = o.y;
+            }
+        } else {
+#pragma unroll
+            for (int p = 0; p < NPOP; ++p) ob[p] = fma(B + kcoef(p), fe[p], P.bw1 * v[p]);
         }
     }
     if (sizeof(T) == 4) {
@@ -521,7 +554,10 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
         // the total mass and momentum.  The momentum defect goes to the +- pair of
         // each axis (mass unchanged), the mass defect to the rest population.
         T r2, mx, my, mz;
-        moments(ob, r2, mx, my, mz);
+        if constexpr (std::is_same<T, float>::value)
+            moments_x2(ob, r2, mx, my, mz);
+        else
+            moments(ob, r2, mx, my, mz);
         T tx = jx, ty = jy, tz = jz;
         if (forced) {
             const T g = r * P.bwF;
@@ -546,9 +582,23 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     const bool small = ny == 1 || nz == 1;  // two images along one axis: copied at the end
     const bool img = !small && (dj != 0 || dk != 0);
     const bool xend = wbase <= 0 || wbase + 31 >= nx - 1;
+    S enc[NPOP];  // the stored values (16-bit forms: deviations of the pairs formed two at a time)
+    if constexpr (Codec<T, S>::deviation) {
+        enc[0] = P.codec.encode_h(0, ob[0], hc);
+#pragma unroll
+        for (int m = 1; m <= 9; ++m) {
+            const int p = 2 * m - 1, q = 2 * m;
+            const float2 d = P.codec.dev2(p, q, make_float2(ob[p], ob[q]));
+            enc[p] = P.codec.encode_dh(p, d.x, hc);
+            enc[q] = P.codec.encode_dh(q, d.y, hc);
+        }
+    } else {
+#pragma unroll
+        for (int p = 0; p < NPOP; ++p) enc[p] = P.codec.encode_h(p, ob[p], hc);
+    }
     if (GHOST == 0 || (!wall_warp && !img && !small && !(P.periodic_x && xend))) {
 #pragma unroll
-        for (int p = 0; p < NPOP; ++p) fb[p * P.ps_b + cb] = P.codec.encode_h(p, ob[p], hc);
+        for (int p = 0; p < NPOP; ++p) fb[p * P.ps_b + cb] = enc[p];
         return;
     }
     __shared__ T wv[4][4][NPOP];  // per warp: values of cells 1, 2, nx, nx-1 (blocks of at most 128 threads)
@@ -566,7 +616,7 @@ __global__ void __launch_bounds__(256) fbar_kernel(const S *__restrict__ f, S *_
     for (int p = 0; p < NPOP; ++p) {
         const T out = ob[p];
         S *pl = fb + p * P.ps_b + rowb;
-        const S e = P.codec.encode_h(p, out, hc);
+        const S e = enc[p];
         if (in) {
             put(pl + ic + 1, e);
             if (P.periodic_x) {

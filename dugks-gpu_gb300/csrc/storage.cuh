@@ -45,9 +45,9 @@ struct Codec {
 
 template <class S>
 struct DevCodec {
-    float w[NPOP];    // rest-state equilibrium w_p (feq(rho=1, u=0))
-    float s[NPOP];    // scale s_p
-    float is[NPOP];   // 1 / s_p
+    PopArr<float> w;  // rest-state equilibrium w_p (feq(rho=1, u=0))
+    PopArr<float> s;  // scale s_p
+    PopArr<float> is; // 1 / s_p
     unsigned sr_seed; // 0: round to nearest, else stochastic rounding with this seed
     static constexpr bool deviation = true;
 };
@@ -124,6 +124,15 @@ struct Codec<float, __half> : DevCodec<__half> {
     {
         return __fmul2_rn(make_float2(s[p], s[q]), x);
     }
+    // dec and the deviation of encode_h for the populations p, q at once
+    __device__ __forceinline__ float2 dec2(int p, int q, float2 x) const
+    {
+        return __ffma2_rn(make_float2(s[p], s[q]), x, make_float2(w[p], w[q]));
+    }
+    __device__ __forceinline__ float2 dev2(int p, int q, float2 v) const
+    {
+        return __fmul2_rn(__fadd2_rn(v, make_float2(-w[p], -w[q])), make_float2(is[p], is[q]));
+    }
     __device__ __forceinline__ float raw(const __half *a, long long idx) const { return __half2float(a[idx]); }
 };
 
@@ -183,6 +192,15 @@ struct Codec<float, __nv_bfloat16> : DevCodec<__nv_bfloat16> {
     __device__ __forceinline__ float2 dec_e2(int p, int q, float2 x) const
     {
         return __fmul2_rn(make_float2(s[p], s[q]), x);
+    }
+    // dec and the deviation of encode_h for the populations p, q at once
+    __device__ __forceinline__ float2 dec2(int p, int q, float2 x) const
+    {
+        return __ffma2_rn(make_float2(s[p], s[q]), x, make_float2(w[p], w[q]));
+    }
+    __device__ __forceinline__ float2 dev2(int p, int q, float2 v) const
+    {
+        return __fmul2_rn(__fadd2_rn(v, make_float2(-w[p], -w[q])), make_float2(is[p], is[q]));
     }
     __device__ __forceinline__ float raw(const __nv_bfloat16 *a, long long idx) const { return __bfloat162float(a[idx]); }
 };
