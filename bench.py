@@ -136,6 +136,14 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
+def launches_per_step(precision, periodic_x):
+    """Kernel launches of one step: stage (a), the flux kernel and, in FP64 and
+    the 16-bit forms with periodic x, the separate ghost pass of f-bar-plus."""
+    if precision == "fp32" or (precision in ("fp16", "bf16") and not periodic_x):
+        return 2
+    return 3
+
+
 def ncu_traffic(precision, grid):
     """DRAM bytes per flux launch from the committed ncu capture of the same
     grid and form (profiles/traffic.json, written from an ncu capture; ncu
@@ -441,7 +449,7 @@ def main():
                 "dtype": {"fp64": "f64", "fp32": "f32", "fp16": "f16-storage/f32", "bf16": "bf16-storage/f32"}[args.precision],
                 "data": "synthetic",
                 "config": bench_config(args, meta, grid, world),
-                "e2e": e2e, "gpu_launches": (2 if args.precision == "fp32" else 3) * K, "roofline": roof, "clocks": clocks}
+                "e2e": e2e, "gpu_launches": launches_per_step(args.precision, periodic_x=False) * K, "roofline": roof, "clocks": clocks}
         line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:

@@ -81,6 +81,31 @@ def test_gradient_reconstruction_fp32_matches_oracle(case):
     assert err <= FP32_TOL
 
 
+@pytest.mark.parametrize("prec", ["fp16", "bf16"])
+@pytest.mark.parametrize("case", ["walls", "stretched"])
+def test_gradient_reconstruction_16bit_matches_oracle(case, prec):
+    """recon=gradient in the 16-bit forms (face values formed from decoded values, carried as
+    f - w like the interpolated ones) within 3 storage quanta of the FP64 oracle."""
+    from _cases import CASES as C
+    import pydugks
+    import pyoracle
+    from seeded import seeded_state
+    kw = dict(C[case])
+    kw["recon"] = "gradient"
+    kw["precision"] = prec
+    cfg = pydugks.make_config(**kw)
+    eng = pydugks.Engine(cfg)
+    orc = pyoracle.Oracle.from_config(cfg)
+    eng.set_state(seeded_state(eng.nx, eng.ny, eng.nz, seed=3))
+    f0 = eng.get_state()
+    got, want = run_both(eng, orc, f0, 1, 10)
+    err = rel_err(got, want)
+    w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+    tol = 3.0 * {"fp16": 2.0 ** -11, "bf16": 2.0 ** -8}[prec] * max(1e-3, float(np.max(np.abs(f0 - w) / w)))
+    print(f"{case} gradient {prec} 10 steps: rel err {err:.3e} (bound {tol:.3e})")
+    assert err <= tol
+
+
 @pytest.mark.parametrize("shape,periodic_x", [((33, 5, 4), 0), ((65, 3, 2), 0), ((20, 1, 3), 0), ((20, 4, 1), 1),
                                               ((9, 1, 1), 0)])
 def test_edge_shapes_match_oracle(shape, periodic_x):
@@ -100,6 +125,38 @@ def test_edge_shapes_match_oracle(shape, periodic_x):
     err = rel_err(got, want)
     print(f"{shape} periodic_x={periodic_x}: rel err {err:.3e}")
     assert err <= FP64_TOL
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp16", "bf16"])
+@pytest.mark.parametrize("shape,periodic_x", [((33, 5, 4), 0), ((65, 3, 2), 0), ((20, 1, 3), 0), ((20, 4, 1), 1),
+                                              ((9, 1, 1), 0), ((40, 9, 3), 0)])
+def test_edge_shapes_float_forms(shape, periodic_x, prec):
+    """The same shapes in the FP32 form (stage (a) writes the ghost layer) and the 16-bit forms
+    (between walls stage (a) writes the y / z images and the flux kernel forms the wall ghost
+    columns in shared memory, in the first tile and in the tile holding column nx).  FP32 within
+    2e-5 of the FP32 oracle; 16-bit within 3 storage quanta of the largest deviation from the
+    rest equilibrium of the FP64 oracle (as tests/test_gpu_mixed.py)."""
+    import pydugks
+    import pyoracle
+    from seeded import seeded_state
+    nx, ny, nz = shape
+    cfg = pydugks.make_config(nx=nx, ny=ny, nz=nz, xwidth=nx, ywidth=ny, zwidth=nz, periods_x=periodic_x,
+                              CFL=0.5, visc=0.02, ambient_fx=1e-5 if periodic_x else 0.0, ambient_fz=1e-5,
+                              precision=prec)
+    eng = pydugks.Engine(cfg)
+    orc = pyoracle.Oracle.from_config(cfg, dtype=np.float32 if prec == "fp32" else np.float64)
+    f0 = seeded_state(nx, ny, nz, seed=9)
+    eng.set_state(f0)
+    f0 = eng.get_state()  # the stored start (16-bit: rounded)
+    got, want = run_both(eng, orc, f0, 1, 10)
+    err = rel_err(got, want)
+    if prec == "fp32":
+        tol = FP32_TOL
+    else:
+        w = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+        tol = 3.0 * {"fp16": 2.0 ** -11, "bf16": 2.0 ** -8}[prec] * max(1e-3, float(np.max(np.abs(f0 - w) / w)))
+    print(f"{shape} periodic_x={periodic_x} {prec}: rel err {err:.3e} (bound {tol:.3e})")
+    assert err <= tol
 
 
 def test_step_is_deterministic():
