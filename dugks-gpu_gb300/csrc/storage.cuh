@@ -3,7 +3,10 @@
 //   Codec<double, double>, Codec<float, float>: plain values (FP64 / FP32 forms)
 //   Codec<float, __half>, Codec<float, __nv_bfloat16>: 16-bit deviations from
 //       the rest-state equilibrium, d_p = (f_p - w_p) / s_p, with one scale s_p
-//       per population; decoded and re-encoded in FP32 (the mixed form).
+//       per population, and FP32 arithmetic (the mixed form): stage (a) decodes
+//       and re-encodes; the flux kernel interpolates the stored deviations,
+//       carries face values as f - w (dec_e) and updates in deviation units
+//       (encode_dh), never forming f itself.
 //       Stochastic rounding when sr_seed != 0 (the default of both forms;
 //       config key rounding=nearest turns it off): hashed bits of (index, population, seed) are added below
 //       the 16-bit mantissa of the float deviation before truncation (16 bits
@@ -11,7 +14,7 @@
 //       not bias time averages; the seed changes every step and the result
 //       stays deterministic.  The step kernels hash the
 //       cell once (cell_hash) and draw the population's bits from it with one
-//       multiply by an odd constant (store_h), a bijection of the hash, so
+//       multiply by an odd constant (encode_dh), a bijection of the hash, so
 //       each population's bits stay uniformly distributed.
 #pragma once
 #include <cuda_fp16.h>
