@@ -46,3 +46,14 @@ def test_single_rank_value():
     import bench
     v, ms = bench.combine_ranks(1, 4194304, 50, 500.0)
     assert ms == 500.0 and abs(v - 4194304 * 50 / 0.5 / 1e6) < 1e-9
+
+
+def test_launch_count_per_form():
+    """The kernels of one step that bench.py's gpu_launches counts: stage (a) and the flux
+    kernel, plus the ghost pass of f-bar-plus in FP64 and in the 16-bit forms with periodic x."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.launches_per_step("fp64", periodic_x=False) == 3
+    assert bench.launches_per_step("fp32", periodic_x=False) == 2
+    assert bench.launches_per_step("fp16", periodic_x=False) == 2
+    assert bench.launches_per_step("bf16", periodic_x=True) == 3
