@@ -248,8 +248,6 @@ struct UpdateSum {
     }
 };
 
-// UpdateSum for the population pair (2m-1, 2m) in FP32 arithmetic, two at a
-// time (FFMA2 / FMUL2): the same operations in the same order for each.
 // The update's pairing rule: the pair (2m-1, 2m) moves along the same axes
 // and sits in adjacent slots of each of their flux lists.
 __host__ __device__ constexpr bool update_pairs_ok()
@@ -265,6 +263,8 @@ __host__ __device__ constexpr bool update_pairs_ok()
 }
 static_assert(update_pairs_ok(), "update population pairs must share their axes and adjacent flux slots");
 
+// UpdateSum for the population pair (2m-1, 2m) in FP32 arithmetic, two at a
+// time (FFMA2 / FMUL2): the same operations in the same order for each.
 template <class S>
 struct UpdatePair {
     float2 r, acc = make_float2(0.0f, 0.0f);
