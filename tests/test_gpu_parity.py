@@ -3,7 +3,7 @@ restatement of the reference step (src/dugks.cu:322-391 and, for the
 stretched mesh, src/fortran/channel/src/dugks.cuf).
 
 Tolerances (max |a-b| / max |b| over f-tilde):
-  FP64 form: 1e-12 per step and over the run (the benchmark spec's bound)
+  FP64 form: 1e-12 per step and over the run (the FP64 parity bound)
   FP32 form: 2e-5 (the reference's PREC4 build itself mixes double literals
              into float expressions, so FP32 parity is not bitwise)
 """

@@ -106,7 +106,7 @@ def _rest_state(nx, ny, nz):
 @pytest.mark.slow
 def test_laminar_channel_matches_reference_over_1e4_steps():
     """FP64 engine vs the reference's kernels: <= 1e-12 relative in f-tilde after
-    1, 100, 1000 and 10^4 steps (the spec parity bound)."""
+    1, 100, 1000 and 10^4 steps (the FP64 parity bound)."""
     _need_ref()
     f0 = _rest_state(64, 32, 32)
     ref = pyoracle.to_ghosted(f0)
